@@ -1,0 +1,344 @@
+"""Benchmark of the delta2zreion step on GB300 (one JSON line on stdout).
+
+Workload (the 512^3 plain configuration): a float32 linear density field at
+z = 0 in a periodic 600 Mpc/h box, N = 512, from Philox4x32-10 white noise
+(seed 1 + rank) shaped by a BBKS P(k) (n_s 0.965, Omega_m 0.31, h 0.68,
+sigma_8 0.81); 64 log-spaced top-hat radii from 2 cells to 60 Mpc/h;
+M_min = 1e9 Msun/h; zeta calibrated so the ionisation midpoint is z ~ 8.
+A step is one delta2zreion pass: the forward R2C of delta_lin and all 64
+radii (window, C2R, barrier, running max) into zreion.
+
+  value : cell*radii/s with delta_lin resident in HBM (CUDA events over K steps)
+  e2e   : the same through the public API with host (pinned) buffers: each step
+          copies delta_lin in and zreion out inside the timed region
+Multi-GPU (torchrun): replicas, one box per rank, no collective on the data
+path; value = all ranks' cell*radii / max-over-ranks time.
+
+--impl reference times the CPU implementation of the same step (the oracle's
+faithful-fp32 restatement: scipy.fft with all host threads plus the OpenMP
+C loops of oracle/d2z_cells.c) on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "pr-calc_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "zreion cell*radii/s at 512^3 (64 radii)"
+UNIT = "cell*radii/s"
+N_DEF, BOX, NR, RMIN_CELLS, RMAX, H_ = 512, 600.0, 64, 2.0, 60.0, 0.68
+MMIN_MSUN = 1e9 / H_
+ZETA = 30.0          # calibrated: x_i(z=8) ~ 0.5 at seed 1
+CPU_SAMPLE_RADII = 4
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _params(N):
+    import prc_d2z
+    p = prc_d2z.Parameters(N=N, Nscales=NR, BoxSize=BOX * N / N_DEF if N != N_DEF else BOX, Rmin=RMIN_CELLS)
+    cl = prc_d2z.CLParameters(Rmax=RMAX, zeta=ZETA, M_min=MMIN_MSUN)
+    return p, cl
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _algo_bytes(kind, N, nb, first):
+    """Algorithmic DRAM bytes of one launch (what the kernel must read + write)."""
+    Nc = N * N * (N // 2 + 1)
+    n3 = N ** 3
+    if kind == "win_x":            # spectrum once, nb slot outputs
+        return 8 * Nc + 8 * Nc * nb
+    if kind == "col_inv":          # nb slots read + written
+        return 16 * Nc * nb
+    if kind == "c2r_z":            # nb slots read, zreion written (+ read after the first sweep)
+        return 8 * Nc * nb + (4 if first else 8) * n3
+    if kind == "r2c_z":
+        return 4 * n3 + 8 * Nc
+    if kind == "col_fwd":
+        return 16 * Nc
+    return None
+
+
+def _traffic(kind, N):
+    """DRAM bytes per launch from the committed ncu summary, or None."""
+    path = os.path.join(REPO, "profiles", f"{kind}_n{N}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_sample(delta_np, tables, box_mpc, n_radii_sample, threads):
+    """Oracle (faithful fp32) on a bounded sample: forward + n radii; returns
+    the extrapolated full-workload cell*radii/s and the timings."""
+    from oracle import d2z_ref as orc
+    orc.lib().orc_set_threads(threads)
+    N = delta_np.shape[0]
+    t0 = time.perf_counter()
+    spec = orc.forward_spectrum(delta_np, tables.DInit, "fp32")
+    t1 = time.perf_counter()
+    zreion = np.zeros(delta_np.shape, np.float32)
+    idx = np.linspace(0, NR - 1, n_radii_sample).round().astype(int)
+    for r in idx:
+        W = orc.window(N, box_mpc, tables.radii_mpc[r], "fp32")
+        dR = orc.smooth(spec, W, N, "fp32")
+        orc.barrier_update(dR, tables.barrier_a, tables.barrier_b[r], int(r), zreion, None, "fp32")
+    t2 = time.perf_counter()
+    t_fwd, t_rad = t1 - t0, (t2 - t1) / len(idx)
+    t_full = t_fwd + NR * t_rad
+    return N ** 3 * NR / t_full, t_fwd, t_rad
+
+
+def run_reference(args, rank):
+    """CPU implementation of the path on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import prc_d2z  # noqa: F401  (tables only; the oracle does the grid work)
+    from oracle import d2z_ref as orc
+    from prc_d2z import fields
+    N = args.n
+    threads = os.cpu_count() or 1
+    p, cl = _params(N)
+    op = orc.Parameters(N=N, Nscales=NR, BoxSize=p.BoxSize, Rmin=RMIN_CELLS, Rmax=RMAX, zeta=ZETA, M_min=MMIN_MSUN)
+    tables = orc.tables(op)
+
+    class T:  # adapter with the field names cpu_sample uses
+        DInit, radii_mpc, barrier_a, barrier_b = tables.DInit, tables.R, tables.A, tables.B
+
+    delta = fields.gaussian_field(N, p.BoxSize, seed=1)
+    box_mpc = float(np.float32(p.BoxSize) / np.float32(H_))
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, tf, tr = cpu_sample(delta, T, box_mpc, args.ref_radii, threads)
+        if s >= args.warmup:
+            vals.append((v, tf, tr))
+    v = statistics.median(x[0] for x in vals)
+    ms = N ** 3 * NR / v * 1e3
+    sample = (f"forward R2C + {args.ref_radii} of {NR} radii per step at {N}^3, extrapolated to all {NR} radii "
+              f"(t_fwd {statistics.median(x[1] for x in vals):.2f} s, t_radius {statistics.median(x[2] for x in vals):.2f} s)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox4x32-10 + BBKS, seed 1)",
+        "config": {"workload": f"plain delta2zreion {N}^3, {p.BoxSize:g} Mpc/h, {NR} radii", "N": N,
+                   "radii": NR, "box_mpc_h": p.BoxSize, "zeta": ZETA, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import prc_d2z
+    from prc_d2z import fields
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    N = args.n
+    p, cl = _params(N)
+    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=args.batch, argmax=False)
+    t = ctx.tables
+    delta = fields.gaussian_field(N, p.BoxSize, seed=1 + rank, backend="torch", device=dev).contiguous()
+    zreion = torch.empty_like(delta)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        ctx.forward(delta, zreion=zreion, want_argmax=False)
+    ctx.profile(True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local_rank) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            ctx.forward(delta, zreion=zreion, want_argmax=False)
+        ev1.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    launches = ctx.last_launches() * args.steps
+    if world > 1:
+        tt = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_step = ms_total / args.steps
+    value = world * N ** 3 * NR / (ms_step * 1e-3)
+
+    # end to end through the public API with pinned host buffers
+    h_delta = torch.empty(delta.shape, dtype=torch.float32, pin_memory=True)
+    h_delta.copy_(delta.cpu())
+    h_z = torch.empty(delta.shape, dtype=torch.float32, pin_memory=True)
+    hd, hz = h_delta.numpy(), h_z.numpy()
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.forward(hd, zreion=hz, want_argmax=False)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.forward(hd, zreion=hz, want_argmax=False)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = world * N ** 3 * NR * args.steps / e2e_s
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel
+    peak, peak_kind = _peaks()
+    B = min(args.batch or 8, NR)
+    sweeps = math.ceil(NR / B)
+    dom = max((k for k in prof if prof[k][1] > 0), key=lambda k: prof[k][0])
+    tot_ms, n_l = prof[dom]
+    per_launch_ms = tot_ms / n_l
+    if dom in ("win_x", "col_inv", "c2r_z"):
+        # average over sweeps: every sweep but possibly the last has B radii
+        byts = [_algo_bytes(dom, N, min(B, NR - s * B), s == 0) for s in range(sweeps)]
+        bytes_launch = sum(byts) / len(byts)
+    else:
+        bytes_launch = _algo_bytes(dom, N, 1, True) or 0
+    achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+    traffic = _traffic(dom, N)
+    rl = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+          "bytes_per_launch": bytes_launch, "ms_per_launch": per_launch_ms,
+          "kernel_share": {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items() if v[1]}}
+    # canonical 3-pass model bytes (40 Nc + 8 N^3 per radius, 4 N^3 + 40 Nc once)
+    Nc = N * N * (N // 2 + 1)
+    canon = NR * (40 * Nc + 8 * N ** 3) + 4 * N ** 3 + 40 * Nc
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox4x32-10 + BBKS, seed 1+rank)",
+        "config": {"workload": f"plain delta2zreion {N}^3, {p.BoxSize:g} Mpc/h, {NR} radii", "N": N,
+                   "radii": NR, "box_mpc_h": p.BoxSize, "zeta": ZETA, "radius_batch": B,
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * N ** 3, "d2h_bytes_per_step": 4 * N ** 3},
+        "gpu_launches": launches,
+        "roofline": rl,
+        "canonical_3pass_gbs": canon / (ms_step * 1e-3) / 1e9,
+        "clocks": clk.summary(),
+    }
+    if world == 1 and not args.no_cpu:
+        from oracle import d2z_ref as orc  # noqa: F401
+        threads = os.cpu_count() or 1
+        d_np = delta.cpu().numpy()
+
+        class T:
+            DInit, radii_mpc, barrier_a, barrier_b = t.DInit, t.radii_mpc, t.barrier_a, t.barrier_b
+
+        v, tf, tr = cpu_sample(d_np, T, float(np.float32(p.BoxSize) / np.float32(H_)), CPU_SAMPLE_RADII, threads)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"oracle fp32: forward R2C ({tf:.2f} s) + {CPU_SAMPLE_RADII} of {NR} radii "
+                                         f"({tr:.2f} s each) at {N}^3, extrapolated to {NR} radii"}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEF)
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--ref-radii", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

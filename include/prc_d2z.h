@@ -1,0 +1,176 @@
+/*
+ * prc_d2z.h — C ABI of the GB300 excursion-set reionization step (delta2zreion).
+ *
+ * The reference executable (pr-calc, c++/src) runs this step as the free function
+ * `void delta2zreion()` (proto_d2z.h:27, delta2zreion_d2z.C:8-204) that talks to
+ * main() only through globals (allvars_d2z.h:33-76) and FFTW-MPI plans
+ * (main_d2z.C:45-48).  This header is the drop-in boundary that replaces that
+ * code: main() keeps its CLI, parameter file, raw float32 grid I/O and the
+ * post-processing, and calls the entry points below instead of
+ * AllocateArrays, the fftwf_mpi_plan_dft_* calls, fftwf_execute and delta2zreion.
+ *
+ * Conventions
+ *   - every entry point returns an int status: PRC_OK (0) or a negative code;
+ *     prc_last_error() returns a message for the calling thread's last failure.
+ *     No entry point calls exit().
+ *   - grids are unpadded, x-major, z fastest (the order of the raw .delta and
+ *     .zreion files, io_d2z.C:164-245): cell (i,j,k) is at i*N*N + j*N + k.
+ *   - pointers flagged "on_device" are CUDA device pointers; otherwise host
+ *     pointers (pinned or pageable) that the call copies through.
+ *   - one context per host thread; calls on one context are serialised on the
+ *     caller-supplied stream.  The library owns its device workspace, the caller
+ *     owns every buffer it passes in.
+ */
+#ifndef PRC_D2Z_H
+#define PRC_D2Z_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define PRC_OK               0
+#define PRC_ERR_INVALID     -1   /* bad argument (size, pointer, radius list) */
+#define PRC_ERR_UNSUPPORTED -2   /* grid size without a compiled FFT plan     */
+#define PRC_ERR_CUDA        -3   /* CUDA runtime error                        */
+#define PRC_ERR_ALLOC       -4   /* device allocation failed                  */
+#define PRC_ERR_IO          -5   /* file could not be opened / short read     */
+#define PRC_ERR_NUMERIC     -6   /* root finder / quadrature did not converge */
+
+/* ---- flags for prc_d2z_desc.flags --------------------------------------- */
+#define PRC_FLAG_ARGMAX      1   /* keep the per-cell winning radius index    */
+#define PRC_FLAG_SIGMA_GRID  2   /* per-radius sqrt(<delta_R^2>) diagnostic   */
+
+#define PRC_NHISTORY      100000 /* allvars_d2z.h:1 */
+#define PRC_ARGMAX_NONE   255    /* argmax value of a cell never updated      */
+#define PRC_MAX_RADII     254
+
+/* ---- host tables (cosmology) -------------------------------------------
+ * Replaces the scalar set-up of delta2zreion_d2z.C:14-38,55,97-100 and
+ * main_d2z.C:57-64: normalize (cosmology.C:246-272), cdmehint
+ * (cosmology.C:214-244), growth (cosmology.C:174-212), inverse_erfc
+ * (math.C:23-61) and d2z's barrier constants (delta2zreion_d2z.C:206-216).
+ * Inputs are the parameter-file and command-line values exactly as the
+ * reference holds them (BoxSize in Mpc/h as read, Rmax in Mpc/h, M_min in
+ * Msun).  Outputs are what the GPU path consumes. */
+typedef struct {
+  float Omegam, Omegab, Omegal, h, ns, sigma8, w;   /* Parameter, allvars_d2z.h:58-64 */
+  float BoxSize;          /* Mpc/h, as in the parameter file                  */
+  float zInit, Rmin;      /* Rmin in cells                                     */
+  int   N, Nscales;
+  float Rmax, zeta, M_min; /* clParameter, allvars_d2z.h:66-70                 */
+} prc_params;
+
+typedef struct {
+  float  DInit, zHigh, DHigh;   /* growth(zInit), 20, growth(20)              */
+  float  pnorm;                 /* sigma8 normalisation                        */
+  float  erfizeta;              /* inverse_erfc(1/zeta)                        */
+  float  sigma_min;             /* sqrt(sigma^2(M_min))                        */
+  double barrier_a;             /* A = (1+zHigh)*DHigh/1.686 (float product)   */
+  /* n = Nscales entries, caller-allocated: */
+  double* radii_mpc;            /* R_r in Mpc (the float the reference uses)  */
+  float*  sigma_r;              /* sigma(R_r)                                  */
+  double* barrier_b;            /* B_r = sqrt(2(smin^2 - s_r^2)) * erfizeta     */
+} prc_tables;
+
+int prc_compute_tables(const prc_params* p, prc_tables* out);
+
+/* Growth factor D(z) (cosmology.C:174-212). */
+float prc_growth(float z, float omegam, float omegal, float w);
+/* sigma^2(M) of a top-hat of mass M [Msun] (cosmology.C:214-244). */
+int prc_sigma2(float omegam, float omegab, float h, float ns, float pnorm,
+               float mass, float* sgm2);
+/* erfc^-1(x) as the reference's bracketing root finder returns it (math.C:23-61). */
+int prc_inverse_erfc(float x, float* out);
+/* Thomson optical depth of an ionisation history (cosmology.C:52-83). */
+float prc_tau(const float* za, const float* xa, int nz, float omegam,
+              float omegab, float h);
+
+/* ---- the GPU path --------------------------------------------------------- */
+typedef struct prc_d2z_ctx prc_d2z_ctx;
+
+typedef struct {
+  int           N;                /* grid side (see prc_d2z_supported)          */
+  int           n_radii;          /* Nscales, 1..PRC_MAX_RADII                  */
+  double        box_mpc;          /* box side in Mpc (BoxSize/h)                */
+  const double* radii_mpc;        /* n_radii top-hat radii [Mpc], processing order */
+  const double* barrier_b;        /* n_radii barrier offsets B_r (NaN: radius never wins) */
+  double        barrier_a;        /* A in z = A*(delta_R + B_r) - 1             */
+  double        growth_init;      /* D(zInit); delta_lin is divided by it (main_d2z.C:59) */
+  int           radius_batch;     /* radii per sweep; 0 = library default       */
+  int           flags;            /* PRC_FLAG_*                                 */
+  void*         stream;           /* cudaStream_t; NULL = default stream        */
+} prc_d2z_desc;
+
+/* 1 if N has a compiled FFT plan, else 0. */
+int prc_d2z_supported(int N);
+
+/* Allocates the device workspace for one box (replaces AllocateArrays,
+ * allocate_d2z.C:5-44, and the FFTW plans, main_d2z.C:32-48). */
+int prc_d2z_create(const prc_d2z_desc* desc, prc_d2z_ctx** out);
+
+/* delta_lin (N^3, file order) -> zreion (N^3) and optional argmax (N^3 uint8,
+ * PRC_ARGMAX_NONE where never updated) and sigma_grid (n_radii doubles).
+ * Replaces main_d2z.C:57-71 (delta/=DInit, forward R2C, delta2zreion()),
+ * i.e. the zreion field before GetHistory/CorrectHistory.  zreion starts at 0
+ * (allocate_d2z.C:464); a radius updates a cell iff its z is strictly larger
+ * (delta2zreion_d2z.C:138). */
+int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_device,
+                    float* zreion, uint8_t* argmax, int out_on_device,
+                    double* sigma_grid);
+
+/* The smoothed field of one radius, delta_R = C2R(W_R * R2C(delta_lin/D_init))/N^3
+ * (delta2zreion_d2z.C:57-93), written to delta_r (N^3).  A diagnostic beside
+ * prc_d2z_forward, which never materialises delta_R. */
+int prc_d2z_smooth(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_device, int radius,
+                   float* delta_r, int out_on_device);
+
+/* Ionisation-history histogram of a zreion grid (bubblehistory_d2z.C:17-34):
+ * counts[PRC_NHISTORY] raw bin counts (optional) and history[PRC_NHISTORY], the
+ * cumulative ionised fraction exactly as GetHistory forms it, and
+ * history_z[PRC_NHISTORY] (optional). */
+int prc_d2z_history(prc_d2z_ctx* ctx, const float* zreion, int zreion_on_device,
+                    uint32_t* counts, float* history, float* history_z);
+
+/* Adjoint of prc_d2z_forward (no reference counterpart: the reference has no
+ * gradient).  dL_dz (N^3) and argmax (N^3) -> dL/d delta_lin (N^3) and
+ * dL/dB_r (n_radii doubles, optional).  The host maps dL/dB_r to dL/dzeta and
+ * dL/dM_min with prc_barrier_grad. */
+int prc_d2z_backward(prc_d2z_ctx* ctx, const float* dL_dz, const uint8_t* argmax,
+                     int in_on_device, float* dL_ddelta, int out_on_device,
+                     double* dL_dB);
+
+/* Time of the last forward/backward split by stage, in milliseconds, measured
+ * with CUDA events on the context's stream: [0] forward R2C, [1] radius sweeps,
+ * [2] total.  Returns PRC_ERR_INVALID if no timed call happened. */
+int prc_d2z_last_timing(prc_d2z_ctx* ctx, float* ms3);
+
+/* Kernel launches issued by the last forward/backward call. */
+int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
+
+/* Per-kernel timing: with profiling enabled every launch is bracketed by CUDA
+ * events on the context's stream and the totals accumulate per kernel kind
+ * (PRC_KIND_*) until the next prc_d2z_profile call resets them. */
+#define PRC_KIND_R2C_Z     0   /* forward z pass (real -> half complex)         */
+#define PRC_KIND_COL_FWD   1   /* forward column pass (y or x)                  */
+#define PRC_KIND_WIN_X     2   /* window + inverse x pass, per sweep            */
+#define PRC_KIND_COL_INV   3   /* inverse column pass (y), per sweep            */
+#define PRC_KIND_C2R_Z     4   /* inverse z pass + barrier/max, per sweep       */
+#define PRC_KIND_ADJ_Z     5   /* adjoint source z pass                         */
+#define PRC_KIND_ADJ_X     6   /* adjoint x pass + window accumulate            */
+#define PRC_KIND_C2R_PLAIN 7   /* plain inverse z pass                          */
+#define PRC_NKINDS         8
+int prc_d2z_profile(prc_d2z_ctx* ctx, int enable);
+int prc_d2z_profile_read(prc_d2z_ctx* ctx, double* ms /*PRC_NKINDS*/, long long* launches /*PRC_NKINDS*/);
+
+int prc_d2z_destroy(prc_d2z_ctx* ctx);
+
+const char* prc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRC_D2Z_H */

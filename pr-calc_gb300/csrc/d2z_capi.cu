@@ -1,0 +1,657 @@
+// d2z_capi.cu — C ABI of the GB300 delta2zreion path (include/prc_d2z.h).
+//
+// Owns the per-box device workspace and sequences the kernels of
+// d2z_kernels.cuh / d2z_adjoint.cuh on the caller's stream:
+//   forward : R2C (z line pass, y and x column passes), then per sweep of up to
+//             B radii: window + x pass -> y pass -> z line pass with barrier/max.
+//   backward: per sweep: source R2C along z -> y pass -> x pass with window
+//             accumulate; then the inverse column passes and a plain z C2R.
+// Replaces AllocateArrays (allocate_d2z.C:5-44), the FFTW plans and executes
+// (main_d2z.C:32-48,67; delta2zreion_d2z.C:92) and the delta2zreion loop.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/prc_d2z.h"
+#include "d2z_adjoint.cuh"
+#include "d2z_dispatch.h"
+#include "errors.h"
+
+namespace prc {
+#define PRC_DECL(NV) const KernelSet* kernel_set_##NV();
+PRC_DECL(8) PRC_DECL(12) PRC_DECL(16) PRC_DECL(24) PRC_DECL(32) PRC_DECL(48) PRC_DECL(64)
+PRC_DECL(96) PRC_DECL(128) PRC_DECL(192) PRC_DECL(256) PRC_DECL(512) PRC_DECL(1024)
+#undef PRC_DECL
+
+const KernelSet* kernel_set(int N) {
+  switch (N) {
+    case 8: return kernel_set_8();
+    case 12: return kernel_set_12();
+    case 16: return kernel_set_16();
+    case 24: return kernel_set_24();
+    case 32: return kernel_set_32();
+    case 48: return kernel_set_48();
+    case 64: return kernel_set_64();
+    case 96: return kernel_set_96();
+    case 128: return kernel_set_128();
+    case 192: return kernel_set_192();
+    case 256: return kernel_set_256();
+    case 512: return kernel_set_512();
+    case 1024: return kernel_set_1024();
+    default: return nullptr;
+  }
+}
+
+// ------------------------------------------------------------ history binning
+// bin = (int)((z - 49.9) / dz), dz = float((0.01 - 49.9)/(1e5 - 1)), evaluated
+// in double exactly as bubblehistory_d2z.C:23 does; a float estimate decides
+// every cell that is not within 0.05 of a bin edge.
+__global__ void k_hist(const float* __restrict__ z, long long n, uint32_t* counts, double dzd) {
+  const float inv = (float)(1.0 / dzd);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long iters = (n + stride - 1) / stride;
+  for (long long it = 0; it < iters; ++it) {
+    const long long i = base + it * stride;
+    const bool valid = i < n;
+    const float zc = valid ? z[i] : 0.f;
+    const float qf = (zc - 49.9f) * inv;
+    int bin = -1;
+    if (fabsf(qf) < 1e9f) {
+      const float r = rintf(qf);
+      if (fabsf(qf - r) < 0.05f)
+        bin = (int)(((double)zc - 49.9) / dzd);
+      else
+        bin = (int)qf;
+    }
+    const bool ok = valid && bin >= 0 && bin < kNHistory;
+    const int key = ok ? bin : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    if (ok && (int)(threadIdx.x & 31) == leader) atomicAdd(&counts[bin], (uint32_t)__popc(peers));
+  }
+}
+
+}  // namespace prc
+
+using namespace prc;
+
+struct prc_d2z_ctx {
+  int N = 0, H = 0, nr = 0, B = 0, flags = 0, dev = 0, sms = 0;
+  long long NN = 0, slot_f2 = 0;
+  double box = 0, A = 0, dinit = 1;
+  std::vector<double> R, Bb;
+  std::vector<float> kr, cb;
+  float as = 0;
+  cudaStream_t st = nullptr;
+  const KernelSet* ks = nullptr;
+  KernelSet ksl{};
+  float2* spec = nullptr;
+  float2* slots = nullptr;
+  float2* tw = nullptr;
+  float* zre = nullptr;
+  uint8_t* am = nullptr;
+  double* sig = nullptr;
+  double* dB = nullptr;
+  uint32_t* counts = nullptr;
+  float* gstage = nullptr;
+  uint8_t* amstage = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float last_ms[3] = {0, 0, 0};
+  int have_timing = 0;
+  int launches = 0;
+  // per-kernel-kind event timing (prc_d2z_profile)
+  int prof = 0;
+  std::vector<cudaEvent_t> pev;   // pairs
+  std::vector<int> pkind;         // kind of each pair
+  size_t pused = 0;
+  double kind_ms[PRC_NKINDS] = {0};
+  long long kind_n[PRC_NKINDS] = {0};
+};
+
+namespace {
+
+// Brackets one launch with a pair of events when profiling is on.
+struct Prof {
+  prc_d2z_ctx* c;
+  size_t i = (size_t)-1;
+  Prof(prc_d2z_ctx* c_, int kind) : c(c_) {
+    if (!c->prof) return;
+    if (c->pused * 2 + 2 > c->pev.size()) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return;
+      c->pev.push_back(a);
+      c->pev.push_back(b);
+      c->pkind.push_back(0);
+    }
+    i = c->pused++;
+    c->pkind[i] = kind;
+    cudaEventRecord(c->pev[2 * i], c->st);
+  }
+  ~Prof() {
+    if (i != (size_t)-1) cudaEventRecord(c->pev[2 * i + 1], c->st);
+  }
+};
+
+// after a stream sync: fold the recorded pairs into the per-kind totals
+void prof_collect(prc_d2z_ctx* c) {
+  for (size_t i = 0; i < c->pused; ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->pev[2 * i], c->pev[2 * i + 1]) == cudaSuccess) {
+      c->kind_ms[c->pkind[i]] += ms;
+      c->kind_n[c->pkind[i]] += 1;
+    }
+  }
+  c->pused = 0;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return prc_fail(PRC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+#define PRC_CU(call, what)                           \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+int grid_for(int items, int per_cta, int occ, int sms) {
+  long long need = (items + per_cta - 1) / per_cta;
+  long long cap = (long long)occ * sms;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
+template <class T> int dalloc(T** p, size_t count, const char* what) {
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return prc_fail(PRC_ERR_ALLOC, "cudaMalloc %s (%zu bytes): %s", what, count * sizeof(T),
+                    cudaGetErrorString(e));
+  }
+  return PRC_OK;
+}
+
+void free_all(prc_d2z_ctx* c) {
+  cudaFree(c->spec);
+  cudaFree(c->slots);
+  cudaFree(c->tw);
+  cudaFree(c->zre);
+  cudaFree(c->am);
+  cudaFree(c->sig);
+  cudaFree(c->dB);
+  cudaFree(c->counts);
+  cudaFree(c->gstage);
+  cudaFree(c->amstage);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->pev) cudaEventDestroy(e);
+  c->pev.clear();
+}
+
+ColSeg seg(const float2* in, float2* out, int rs, int os, int no, int ncp, int tr) {
+  ColSeg s;
+  s.in = in;
+  s.out = out;
+  s.row_stride = rs;
+  s.outer_stride = os;
+  s.n_outer = no;
+  s.n_cp = ncp;
+  s.transpose = tr;
+  return s;
+}
+
+// one column pass over the main array and the Nyquist plane
+void run_col(prc_d2z_ctx* c, bool inv, ColSeg s0, ColSeg s1, int nslots) {
+  ColArgs a;
+  a.seg[0] = s0;
+  a.seg[1] = s1;
+  a.slot_stride = c->slot_f2;
+  a.tw = c->tw;
+  const int items = s0.n_outer * s0.n_cp + s1.n_outer * s1.n_cp;
+  dim3 grid(grid_for(items, c->ksl.col_groups, c->ksl.occ_col, c->sms), nslots, 1);
+  {
+    Prof pf(c, inv ? PRC_KIND_COL_INV : PRC_KIND_COL_FWD);
+    c->ks->col(c->ksl, inv, grid, c->st, a);
+  }
+  c->launches++;
+}
+
+int check_ctx(prc_d2z_ctx* c) {
+  if (!c || !c->ks) return prc_fail(PRC_ERR_INVALID, "null or destroyed context");
+  return PRC_OK;
+}
+
+int set_device(prc_d2z_ctx* c) {
+  int cur = -1;
+  PRC_CU(cudaGetDevice(&cur), "cudaGetDevice");
+  if (cur != c->dev) PRC_CU(cudaSetDevice(c->dev), "cudaSetDevice");
+  return PRC_OK;
+}
+
+// R2C of delta_lin (device) into c->spec.
+void forward_r2c(prc_d2z_ctx* c, const float* d_delta) {
+  const int N = c->N, H = c->H;
+  const long long NN = c->NN;
+  float2* S = c->spec;
+  float2* Q = c->spec + NN * H;
+  float2* Qt = c->spec + NN * (H + 1);  // scratch after the Nyquist plane
+  {
+    Prof pf(c, PRC_KIND_R2C_Z);
+    c->ks->r2c_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_r2c, c->sms), c->st, d_delta,
+                 (float)c->dinit, S, Qt, c->tw);
+  }
+  c->launches++;
+  // y pass: main in place; Nyquist Qt[iy][ix] -> Q[ix][ky]
+  run_col(c, false, seg(S, S, H, N * H, N, H / 2, 0), seg(Qt, Q, N, 0, 1, N / 2, 1), 1);
+  // x pass: main in place; Nyquist Q in place
+  run_col(c, false, seg(S, S, N * H, H, N, H / 2, 0), seg(Q, Q, N, 0, 1, N / 2, 0), 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int prc_d2z_supported(int N) { return kernel_set(N) != nullptr ? 1 : 0; }
+
+int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
+  if (!d || !out) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: null argument");
+  *out = nullptr;
+  const KernelSet* ks = kernel_set(d->N);
+  if (!ks) return prc_fail(PRC_ERR_UNSUPPORTED, "prc_d2z_create: no FFT plan for N=%d", d->N);
+  if (d->n_radii < 1 || d->n_radii > PRC_MAX_RADII)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: n_radii=%d outside 1..%d", d->n_radii, PRC_MAX_RADII);
+  if (!d->radii_mpc || !d->barrier_b) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: null radius table");
+  if (!(d->box_mpc > 0)) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: box_mpc must be > 0");
+  if (!(d->growth_init > 0)) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: growth factor must be > 0");
+  if (!(d->barrier_a > 0)) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: barrier_a must be > 0");
+  for (int r = 0; r < d->n_radii; ++r)
+    if (!(d->radii_mpc[r] > 0)) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: radius %d not > 0", r);
+  if (d->radius_batch < 0 || d->radius_batch > kMaxBatch)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: radius_batch must be 0..%d", kMaxBatch);
+
+  prc_d2z_ctx* c = new prc_d2z_ctx();
+  c->N = d->N;
+  c->H = d->N / 2;
+  c->nr = d->n_radii;
+  c->flags = d->flags;
+  c->NN = (long long)d->N * d->N;
+  c->slot_f2 = c->NN * (c->H + 2);
+  c->box = d->box_mpc;
+  c->A = d->barrier_a;
+  c->dinit = d->growth_init;
+  c->st = (cudaStream_t)d->stream;
+  c->ks = ks;
+  c->ksl = *ks;
+  int B = d->radius_batch ? d->radius_batch : 8;
+  if (B > c->nr) B = c->nr;
+  c->B = B;
+  const double dk = 2.0 * M_PI / d->box_mpc;
+  const double n3 = (double)d->N * d->N * d->N;
+  c->as = (float)(d->barrier_a / n3);
+  for (int r = 0; r < c->nr; ++r) {
+    c->R.push_back(d->radii_mpc[r]);
+    c->Bb.push_back(d->barrier_b[r]);
+    c->kr.push_back((float)(dk * d->radii_mpc[r]));
+    c->cb.push_back((float)(d->barrier_a * d->barrier_b[r] - 1.0));
+  }
+  int st;
+  cudaError_t e = cudaGetDevice(&c->dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev);
+  if (e == cudaSuccess) e = ks->init(&c->ksl);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "prc_d2z_create: device set-up");
+  }
+  const long long n3l = (long long)c->NN * c->N;
+  if ((st = dalloc(&c->spec, (size_t)c->slot_f2, "spectrum")) != PRC_OK ||
+      (st = dalloc(&c->slots, (size_t)c->slot_f2 * c->B, "radius slots")) != PRC_OK ||
+      (st = dalloc(&c->tw, (size_t)c->N, "twiddles")) != PRC_OK ||
+      (st = dalloc(&c->sig, (size_t)c->nr, "sigma accumulators")) != PRC_OK ||
+      (st = dalloc(&c->dB, (size_t)c->nr, "barrier gradient")) != PRC_OK ||
+      (st = dalloc(&c->counts, (size_t)kNHistory, "history counts")) != PRC_OK) {
+    free_all(c);
+    delete c;
+    return st;
+  }
+  (void)n3l;
+  // twiddles e^{+2 pi i k/N}, FP64 on the host
+  std::vector<float2> tw(c->N);
+  for (int k = 0; k < c->N; ++k) {
+    const double ang = 2.0 * M_PI * (double)k / (double)c->N;
+    tw[k] = make_float2((float)cos(ang), (float)sin(ang));
+  }
+  e = cudaMemcpy(c->tw, tw.data(), sizeof(float2) * c->N, cudaMemcpyHostToDevice);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  if (e != cudaSuccess) {
+    free_all(c);
+    delete c;
+    return cuda_fail(e, "prc_d2z_create: upload");
+  }
+  *out = c;
+  return PRC_OK;
+}
+
+int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, float* zreion,
+                    uint8_t* argmax, int out_on_device, double* sigma_grid) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!delta_lin || !zreion) return prc_fail(PRC_ERR_INVALID, "prc_d2z_forward: null delta or zreion");
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const int N = c->N, H = c->H;
+  const long long NN = c->NN, n3 = NN * N;
+  c->launches = 0;
+  c->have_timing = 0;
+  // device buffers
+  const float* d_delta = delta_lin;
+  if (!delta_on_device) {
+    float* stage = reinterpret_cast<float*>(c->slots);  // slot 0 main region holds N^3 floats
+    PRC_CU(cudaMemcpyAsync(stage, delta_lin, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D delta");
+    d_delta = stage;
+  }
+  float* d_z = zreion;
+  uint8_t* d_am = argmax;
+  const bool want_am = argmax != nullptr || (c->flags & PRC_FLAG_ARGMAX);
+  if (!out_on_device || (want_am && !argmax)) {
+    if (!out_on_device && !c->zre && (st = dalloc(&c->zre, (size_t)n3, "zreion")) != PRC_OK) return st;
+    if (want_am && !c->am && (st = dalloc(&c->am, (size_t)n3, "argmax")) != PRC_OK) return st;
+    if (!out_on_device) d_z = c->zre;
+    if (want_am && (!out_on_device || !argmax)) d_am = c->am;
+  }
+  if (!want_am) d_am = nullptr;
+  const bool want_sig = sigma_grid != nullptr || (c->flags & PRC_FLAG_SIGMA_GRID);
+  if (want_sig) PRC_CU(cudaMemsetAsync(c->sig, 0, sizeof(double) * c->nr, c->st), "memset sigma");
+
+  PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
+  forward_r2c(c, d_delta);
+  PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
+  for (int r0 = 0; r0 < c->nr; r0 += c->B) {
+    const int nb = (c->nr - r0 < c->B) ? c->nr - r0 : c->B;
+    SweepArgs sa;
+    memset(&sa, 0, sizeof(sa));
+    sa.spec = c->spec;
+    sa.slots = c->slots;
+    sa.slot_stride = c->slot_f2;
+    sa.tw = c->tw;
+    sa.zreion = d_z;
+    sa.argmax = d_am;
+    sa.sig_acc = want_sig ? c->sig : nullptr;
+    sa.nb = nb;
+    sa.r0 = r0;
+    sa.first = (r0 == 0);
+    sa.as = c->as;
+    for (int b = 0; b < nb; ++b) {
+      sa.kr[b] = c->kr[r0 + b];
+      sa.cb[b] = c->cb[r0 + b];
+    }
+    {
+      Prof pf(c, PRC_KIND_WIN_X);
+      c->ks->win_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_win, c->sms), c->st, sa);
+    }
+    c->launches++;
+    float2* U = c->slots;
+    run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), nb);
+    {
+      Prof pf(c, PRC_KIND_C2R_Z);
+      c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, sa);
+    }
+    c->launches++;
+  }
+  PRC_CU(cudaGetLastError(), "kernel launch");
+  PRC_CU(cudaEventRecord(c->ev[2], c->st), "event");
+  if (!out_on_device) {
+    PRC_CU(cudaMemcpyAsync(zreion, d_z, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H zreion");
+    if (argmax) PRC_CU(cudaMemcpyAsync(argmax, d_am, n3, cudaMemcpyDeviceToHost, c->st), "D2H argmax");
+  } else if (argmax && d_am != argmax) {
+    PRC_CU(cudaMemcpyAsync(argmax, d_am, n3, cudaMemcpyDeviceToDevice, c->st), "D2D argmax");
+  }
+  std::vector<double> sig;
+  if (sigma_grid) {
+    sig.resize(c->nr);
+    PRC_CU(cudaMemcpyAsync(sig.data(), c->sig, sizeof(double) * c->nr, cudaMemcpyDeviceToHost, c->st), "D2H sigma");
+  }
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_forward");
+  prof_collect(c);
+  float t0, t1;
+  PRC_CU(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]), "event time");
+  PRC_CU(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]), "event time");
+  c->last_ms[0] = t0;
+  c->last_ms[1] = t1;
+  c->last_ms[2] = t0 + t1;
+  c->have_timing = 1;
+  if (sigma_grid) {
+    // GetMeanSigma (arrayoperations.C:4-35): sqrt(<delta_R^2>), delta_R = x / N^3
+    const double n3d = (double)n3;
+    for (int r = 0; r < c->nr; ++r) sigma_grid[r] = sqrt(sig[r] / (n3d * n3d * n3d));
+  }
+  return PRC_OK;
+}
+
+int prc_d2z_smooth(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, int radius, float* delta_r,
+                   int out_on_device) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!delta_lin || !delta_r) return prc_fail(PRC_ERR_INVALID, "prc_d2z_smooth: null argument");
+  if (radius < 0 || radius >= c->nr) return prc_fail(PRC_ERR_INVALID, "prc_d2z_smooth: radius %d out of range", radius);
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const int N = c->N, H = c->H;
+  const long long NN = c->NN, n3 = NN * N;
+  c->launches = 0;
+  const float* d_delta = delta_lin;
+  if (!delta_on_device) {
+    float* stage = reinterpret_cast<float*>(c->slots);
+    PRC_CU(cudaMemcpyAsync(stage, delta_lin, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D delta");
+    d_delta = stage;
+  }
+  float* d_out = delta_r;
+  if (!out_on_device) {
+    if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "output stage")) != PRC_OK) return st;
+    d_out = c->zre;
+  }
+  forward_r2c(c, d_delta);
+  SweepArgs sa;
+  memset(&sa, 0, sizeof(sa));
+  sa.spec = c->spec;
+  sa.slots = c->slots;
+  sa.slot_stride = c->slot_f2;
+  sa.tw = c->tw;
+  sa.nb = 1;
+  sa.r0 = radius;
+  sa.kr[0] = c->kr[radius];
+  c->ks->win_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_win, c->sms), c->st, sa);
+  c->launches++;
+  float2* U = c->slots;
+  run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), 1);
+  AdjArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  fa.slots = U;
+  fa.tw = c->tw;
+  fa.out = d_out;
+  fa.scale = (float)(1.0 / (double)n3);
+  c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, fa);
+  c->launches++;
+  PRC_CU(cudaGetLastError(), "kernel launch");
+  if (!out_on_device)
+    PRC_CU(cudaMemcpyAsync(delta_r, d_out, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H delta_R");
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_smooth");
+  prof_collect(c);
+  return PRC_OK;
+}
+
+int prc_d2z_history(prc_d2z_ctx* c, const float* zreion, int zreion_on_device, uint32_t* counts,
+                    float* history, float* history_z) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!zreion || !history) return prc_fail(PRC_ERR_INVALID, "prc_d2z_history: null zreion or history");
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const long long n3 = c->NN * c->N;
+  const float* d_z = zreion;
+  if (!zreion_on_device) {
+    if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "zreion")) != PRC_OK) return st;
+    PRC_CU(cudaMemcpyAsync(c->zre, zreion, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D zreion");
+    d_z = c->zre;
+  }
+  PRC_CU(cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * kNHistory, c->st), "memset counts");
+  const float dzf = (float)((0.01 - 49.9) / (100000 - 1));  // allvars_d2z.h:1-3, bubblehistory_d2z.C:11
+  int blocks = c->sms * 8;
+  k_hist<<<blocks, 256, 0, c->st>>>(d_z, n3, c->counts, (double)dzf);
+  PRC_CU(cudaGetLastError(), "k_hist launch");
+  std::vector<uint32_t> h(kNHistory);
+  PRC_CU(cudaMemcpyAsync(h.data(), c->counts, sizeof(uint32_t) * kNHistory, cudaMemcpyDeviceToHost, c->st),
+         "D2H counts");
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_history");
+  if (counts) memcpy(counts, h.data(), sizeof(uint32_t) * kNHistory);
+  // bubblehistory_d2z.C:30-34: float counts / N^3 (double), then a float running sum
+  const double n3d = pow((double)c->N, 3.0);
+  for (int i = 0; i < kNHistory; ++i) history[i] = (float)((double)(float)h[i] / n3d);
+  for (int i = 1; i < kNHistory; ++i) history[i] += history[i - 1];
+  if (history_z) {
+    history_z[0] = (float)49.9;
+    for (int i = 1; i < kNHistory; ++i) history_z[i] = (float)(49.9 + i * (double)dzf);
+  }
+  return PRC_OK;
+}
+
+int prc_d2z_backward(prc_d2z_ctx* c, const float* dL_dz, const uint8_t* argmax, int in_on_device,
+                     float* dL_ddelta, int out_on_device, double* dL_dB) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!dL_dz || !argmax || !dL_ddelta) return prc_fail(PRC_ERR_INVALID, "prc_d2z_backward: null argument");
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const int N = c->N, H = c->H;
+  const long long NN = c->NN, n3 = NN * N;
+  c->launches = 0;
+  c->have_timing = 0;
+  const float* d_g = dL_dz;
+  const uint8_t* d_am = argmax;
+  if (!in_on_device) {
+    if (!c->gstage && (st = dalloc(&c->gstage, (size_t)n3, "gradient stage")) != PRC_OK) return st;
+    if (!c->amstage && (st = dalloc(&c->amstage, (size_t)n3, "argmax stage")) != PRC_OK) return st;
+    PRC_CU(cudaMemcpyAsync(c->gstage, dL_dz, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D dL/dz");
+    PRC_CU(cudaMemcpyAsync(c->amstage, argmax, n3, cudaMemcpyHostToDevice, c->st), "H2D argmax");
+    d_g = c->gstage;
+    d_am = c->amstage;
+  }
+  float* d_out = dL_ddelta;
+  if (!out_on_device) {
+    if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "output stage")) != PRC_OK) return st;
+    d_out = c->zre;
+  }
+  if (dL_dB) PRC_CU(cudaMemsetAsync(c->dB, 0, sizeof(double) * c->nr, c->st), "memset dB");
+  PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
+  float2* U = c->slots;
+  float2* acc = c->spec;
+  for (int r0 = 0; r0 < c->nr; r0 += c->B) {
+    const int nb = (c->nr - r0 < c->B) ? c->nr - r0 : c->B;
+    AdjArgs aa;
+    memset(&aa, 0, sizeof(aa));
+    aa.g = d_g;
+    aa.am = d_am;
+    aa.A = (float)c->A;
+    aa.slots = U;
+    aa.slot_stride = c->slot_f2;
+    aa.acc = acc;
+    aa.tw = c->tw;
+    aa.dB = dL_dB ? c->dB : nullptr;
+    aa.nb = nb;
+    aa.r0 = r0;
+    aa.first = (r0 == 0);
+    for (int b = 0; b < nb; ++b) aa.kr[b] = c->kr[r0 + b];
+    {
+      Prof pf(c, PRC_KIND_ADJ_Z);
+      c->ks->adj_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_adj_z, c->sms), c->st, aa);
+    }
+    c->launches++;
+    // forward y pass of each slot; Nyquist scratch Qt_b -> Q_b[ix][ky]
+    run_col(c, false, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * (H + 1), U + NN * H, N, 0, 1, N / 2, 1), nb);
+    {
+      Prof pf(c, PRC_KIND_ADJ_X);
+      c->ks->adj_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_adj_x, c->sms), c->st, aa);
+    }
+    c->launches++;
+  }
+  PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
+  // inverse of the accumulated spectrum into slot 0, then the z C2R
+  run_col(c, true, seg(acc, U, N * H, H, N, H / 2, 0), seg(acc + NN * H, U + NN * H, N, 0, 1, N / 2, 1), 1);
+  run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), 1);
+  AdjArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  fa.slots = U;
+  fa.tw = c->tw;
+  fa.out = d_out;
+  fa.scale = (float)(1.0 / ((double)n3 * c->dinit));
+  {
+    Prof pf(c, PRC_KIND_C2R_PLAIN);
+    c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, fa);
+  }
+  c->launches++;
+  PRC_CU(cudaGetLastError(), "kernel launch");
+  PRC_CU(cudaEventRecord(c->ev[2], c->st), "event");
+  if (!out_on_device)
+    PRC_CU(cudaMemcpyAsync(dL_ddelta, d_out, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H gradient");
+  if (dL_dB) PRC_CU(cudaMemcpyAsync(dL_dB, c->dB, sizeof(double) * c->nr, cudaMemcpyDeviceToHost, c->st), "D2H dB");
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_backward");
+  prof_collect(c);
+  float t0, t1;
+  PRC_CU(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]), "event time");
+  PRC_CU(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]), "event time");
+  c->last_ms[0] = t1;
+  c->last_ms[1] = t0;
+  c->last_ms[2] = t0 + t1;
+  c->have_timing = 1;
+  return PRC_OK;
+}
+
+int prc_d2z_last_timing(prc_d2z_ctx* c, float* ms3) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!ms3 || !c->have_timing) return prc_fail(PRC_ERR_INVALID, "prc_d2z_last_timing: no timed call");
+  for (int i = 0; i < 3; ++i) ms3[i] = c->last_ms[i];
+  return PRC_OK;
+}
+
+int prc_d2z_last_launches(prc_d2z_ctx* c, int* n) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!n) return prc_fail(PRC_ERR_INVALID, "prc_d2z_last_launches: null output");
+  *n = c->launches;
+  return PRC_OK;
+}
+
+int prc_d2z_profile(prc_d2z_ctx* c, int enable) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  c->prof = enable ? 1 : 0;
+  for (int k = 0; k < PRC_NKINDS; ++k) {
+    c->kind_ms[k] = 0;
+    c->kind_n[k] = 0;
+  }
+  c->pused = 0;
+  return PRC_OK;
+}
+
+int prc_d2z_profile_read(prc_d2z_ctx* c, double* ms, long long* launches) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!ms || !launches) return prc_fail(PRC_ERR_INVALID, "prc_d2z_profile_read: null output");
+  for (int k = 0; k < PRC_NKINDS; ++k) {
+    ms[k] = c->kind_ms[k];
+    launches[k] = c->kind_n[k];
+  }
+  return PRC_OK;
+}
+
+int prc_d2z_destroy(prc_d2z_ctx* c) {
+  if (!c) return PRC_OK;
+  set_device(c);
+  if (c->st) cudaStreamSynchronize(c->st);
+  free_all(c);
+  c->ks = nullptr;
+  delete c;
+  return PRC_OK;
+}
+
+}  // extern "C"

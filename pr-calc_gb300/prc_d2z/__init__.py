@@ -1,0 +1,362 @@
+"""prc_d2z -- the excursion-set reionization step (pr-calc's delta2zreion) on
+one GB300, called through the C ABI of libprc_d2z.so.
+
+Host-side mirror of the reference's interface for this path (pr-calc c++/src):
+
+  Parameters / CLParameters  the structs of allvars_d2z.h:58-70, same names
+  read_parameter_file        io_d2z.C:16-162 (tags, comments, -usedvalues echo)
+  compute_tables             delta2zreion_d2z.C:14-38,55,97-100 and
+                             main_d2z.C:57-64 through prc_compute_tables
+  Delta2Zreion               the device context: forward() replaces
+                             main_d2z.C:57-71 + delta2zreion(), history()
+                             GetHistory (bubblehistory_d2z.C:5-43), backward()
+                             the adjoint (new)
+  delta2zreion               one call from delta_lin to (zreion, argmax,
+                             sigma_grid), like the reference's function
+
+Arrays may be numpy arrays (host; the library copies through) or CUDA torch
+tensors (device pointers, no copies).  Everything runs on the GPU; without the
+built library every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import (PRC_ARGMAX_NONE, PRC_FLAG_ARGMAX, PRC_FLAG_SIGMA_GRID, PRC_NHISTORY, PrcError,
+                   check, load)
+
+__all__ = ["Parameters", "CLParameters", "Tables", "read_parameter_file", "compute_tables",
+           "Delta2Zreion", "delta2zreion", "PrcError", "PRC_ARGMAX_NONE", "PRC_NHISTORY",
+           "supported_sizes", "growth", "inverse_erfc", "tau"]
+
+
+@dataclass
+class Parameters:
+    """Parameter (allvars_d2z.h:58-64); BoxSize in Mpc/h as read."""
+    Omegam: float = 0.31
+    Omegab: float = 0.049
+    Omegal: float = 0.69
+    h: float = 0.68
+    ns: float = 0.965
+    sigma8: float = 0.81
+    w: float = -1.0
+    BoxSize: float = 200.0
+    zInit: float = 0.0
+    Rmin: float = 2.0
+    N: int = 128
+    Nscales: int = 32
+    DeltaFile: str = ""
+    RecordBubbleSizes: int = 0
+
+
+@dataclass
+class CLParameters:
+    """clParameter (allvars_d2z.h:66-70) with the defaults of commandline_d2z.C:47-52."""
+    Rmax: float = 256.0
+    zeta: float = 10.0
+    M_min: float = 1e8
+    verbose: int = 0
+    everbose: int = 0
+    lean: int = 0
+    Paramfile: str = ""
+    Basename: str = "output/output"
+
+
+@dataclass
+class Tables:
+    DInit: float
+    zHigh: float
+    DHigh: float
+    pnorm: float
+    erfizeta: float
+    sigma_min: float
+    barrier_a: float
+    radii_mpc: np.ndarray = field(repr=False)
+    sigma_r: np.ndarray = field(repr=False)
+    barrier_b: np.ndarray = field(repr=False)
+
+
+_TAGS = {"Omegam": "f", "Omegab": "f", "Omegal": "f", "h": "f", "ns": "f", "sigma8": "f", "w": "f",
+         "BoxSize": "f", "zInit": "f", "Rmin": "f", "N": "i", "Nscales": "i", "DeltaFile": "s",
+         "RecordBubbleSizes": "i"}
+
+
+def _atof(s: str) -> float:
+    import re
+    m = re.match(r"\s*[+-]?(\d+\.?\d*([eE][+-]?\d+)?|\.\d+([eE][+-]?\d+)?)", s)
+    return float(np.float32(float(m.group(0)))) if m else 0.0
+
+
+def _atoi(s: str) -> int:
+    import re
+    m = re.match(r"\s*[+-]?\d+", s)
+    return int(m.group(0)) if m else 0
+
+
+def read_parameter_file(path: str, echo: bool = True) -> tuple[Parameters, list[str]]:
+    """io_d2z.C:16-162.  Unknown or repeated tags are reported and skipped;
+    the values used are echoed to `<path>-usedvalues`.  Raises OSError when the
+    file cannot be opened (the reference only prints, io_d2z.C:150-153)."""
+    p = Parameters()
+    seen: set[str] = set()
+    errors: list[str] = []
+    lines_out = []
+    with open(path) as fh:
+        for line in fh:
+            tok = line.split()
+            if len(tok) < 2 or tok[0][0] in "%#":
+                continue
+            key, val = tok[0], tok[1]
+            if key not in _TAGS or key in seen:
+                errors.append(f"Error in {path}: Tag '{key}' not allowed or multiple defined.")
+                continue
+            seen.add(key)
+            t = _TAGS[key]
+            if t == "f":
+                setattr(p, key, _atof(val))
+                lines_out.append(f"{key:<35s}{getattr(p, key):f}\n")
+            elif t == "i":
+                setattr(p, key, _atoi(val))
+                lines_out.append(f"{key:<35s}{getattr(p, key):d}\n")
+            else:
+                setattr(p, key, val)
+                lines_out.append(f"{key:<35s}{val}\n")
+    if echo:
+        with open(path + "-usedvalues", "w") as fo:
+            fo.writelines(lines_out)
+    return p, errors
+
+
+def growth(z: float, omegam: float, omegal: float, w: float) -> float:
+    """Growth factor D(z), cosmology.C:174-212."""
+    return float(load().prc_growth(z, omegam, omegal, w))
+
+
+def inverse_erfc(x: float) -> float:
+    """erfc^-1 as math.C:23-61 returns it (low end of a 1e-4 bracket)."""
+    out = ctypes.c_float()
+    check(load().prc_inverse_erfc(x, ctypes.byref(out)))
+    return float(out.value)
+
+
+def tau(history_z: np.ndarray, history: np.ndarray, omegam: float, omegab: float, h: float) -> float:
+    """Thomson optical depth of an ionisation history, cosmology.C:52-83."""
+    za = np.ascontiguousarray(history_z, np.float32)
+    xa = np.ascontiguousarray(history, np.float32)
+    return float(load().prc_tau(za.ctypes.data, xa.ctypes.data, len(za), omegam, omegab, h))
+
+
+def compute_tables(p: Parameters, cl: CLParameters) -> Tables:
+    """Host tables of the step (FP32/FP64 as the reference keeps them)."""
+    L = load()
+    pp = _lib.prc_params(p.Omegam, p.Omegab, p.Omegal, p.h, p.ns, p.sigma8, p.w, p.BoxSize, p.zInit,
+                         p.Rmin, p.N, p.Nscales, cl.Rmax, cl.zeta, cl.M_min)
+    R = np.zeros(p.Nscales, np.float64)
+    S = np.zeros(p.Nscales, np.float32)
+    B = np.zeros(p.Nscales, np.float64)
+    t = _lib.prc_tables()
+    t.radii_mpc = R.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    t.sigma_r = S.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    t.barrier_b = B.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    check(L.prc_compute_tables(ctypes.byref(pp), ctypes.byref(t)))
+    return Tables(t.DInit, t.zHigh, t.DHigh, t.pnorm, t.erfizeta, t.sigma_min, t.barrier_a, R, S, B)
+
+
+def supported_sizes() -> list[int]:
+    L = load()
+    return [n for n in range(2, 2049) if L.prc_d2z_supported(n)]
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _dev_ptr(x, dtype_name: str, n: int):
+    if not x.is_cuda:
+        raise ValueError("torch tensors passed to prc_d2z must live on a CUDA device")
+    if not x.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    if str(x.dtype) != f"torch.{dtype_name}" or x.numel() != n:
+        raise ValueError(f"expected {n} elements of {dtype_name}, got {x.numel()} of {x.dtype}")
+    return ctypes.c_void_p(x.data_ptr())
+
+
+def _host_ptr(x, dtype, n: int):
+    if not isinstance(x, np.ndarray) or x.dtype != dtype or x.size != n or not x.flags.c_contiguous:
+        raise ValueError(f"expected a contiguous numpy array of {n} {np.dtype(dtype).name}")
+    return ctypes.c_void_p(x.ctypes.data)
+
+
+class Delta2Zreion:
+    """One box on the GPU (prc_d2z_create .. prc_d2z_destroy)."""
+
+    def __init__(self, N: int, box_mpc: float, radii_mpc, barrier_b, barrier_a: float, growth_init: float = 1.0,
+                 radius_batch: int = 0, argmax: bool = True, sigma_grid: bool = False, stream=None):
+        L = load()
+        self.N = int(N)
+        self.n3 = self.N ** 3
+        self.radii = np.ascontiguousarray(radii_mpc, np.float64)
+        self.barrier_b = np.ascontiguousarray(barrier_b, np.float64)
+        self.n_radii = len(self.radii)
+        self.barrier_a = float(barrier_a)
+        self.growth_init = float(growth_init)
+        d = _lib.prc_d2z_desc()
+        d.N = self.N
+        d.n_radii = self.n_radii
+        d.box_mpc = float(box_mpc)
+        d.radii_mpc = self.radii.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.barrier_b = self.barrier_b.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.barrier_a = self.barrier_a
+        d.growth_init = self.growth_init
+        d.radius_batch = int(radius_batch)
+        d.flags = (PRC_FLAG_ARGMAX if argmax else 0) | (PRC_FLAG_SIGMA_GRID if sigma_grid else 0)
+        d.stream = ctypes.c_void_p(int(stream)) if stream is not None else None
+        self._ctx = ctypes.c_void_p()
+        check(L.prc_d2z_create(ctypes.byref(d), ctypes.byref(self._ctx)))
+
+    @classmethod
+    def from_parameters(cls, p: Parameters, cl: CLParameters, **kw) -> "Delta2Zreion":
+        t = compute_tables(p, cl)
+        obj = cls(p.N, float(np.float32(p.BoxSize) / np.float32(p.h)), t.radii_mpc, t.barrier_b, t.barrier_a,
+                  t.DInit, **kw)
+        obj.tables = t
+        return obj
+
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            load().prc_d2z_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------------- forward
+    def forward(self, delta_lin, zreion=None, argmax=None, want_argmax: bool = True,
+                want_sigma_grid: bool = False):
+        """delta_lin (N^3 float32, file order) -> (zreion, argmax | None, sigma_grid | None).
+
+        numpy in -> numpy out (host copies inside the call); CUDA tensor in ->
+        CUDA tensors out (no copies)."""
+        L = load()
+        n3 = self.n3
+        sig = np.zeros(self.n_radii, np.float64) if want_sigma_grid else None
+        sig_p = ctypes.c_void_p(sig.ctypes.data) if sig is not None else None
+        if _is_torch(delta_lin):
+            import torch
+            dp = _dev_ptr(delta_lin.reshape(-1), "float32", n3)
+            if zreion is None:
+                zreion = torch.empty(delta_lin.shape, dtype=torch.float32, device=delta_lin.device)
+            if want_argmax and argmax is None:
+                argmax = torch.empty(delta_lin.shape, dtype=torch.uint8, device=delta_lin.device)
+            zp = _dev_ptr(zreion.reshape(-1), "float32", n3)
+            ap = _dev_ptr(argmax.reshape(-1), "uint8", n3) if argmax is not None else None
+            check(L.prc_d2z_forward(self._ctx, dp, 1, zp, ap, 1, sig_p))
+        else:
+            d = np.ascontiguousarray(delta_lin, np.float32)
+            dp = _host_ptr(d, np.float32, n3)
+            if zreion is None:
+                zreion = np.empty(d.shape, np.float32)
+            if want_argmax and argmax is None:
+                argmax = np.empty(d.shape, np.uint8)
+            zp = _host_ptr(zreion, np.float32, n3)
+            ap = _host_ptr(argmax, np.uint8, n3) if argmax is not None else None
+            check(L.prc_d2z_forward(self._ctx, dp, 0, zp, ap, 0, sig_p))
+        return zreion, argmax, sig
+
+    def smooth(self, delta_lin, radius: int):
+        """delta_R of one radius (diagnostic; host or device like forward)."""
+        L = load()
+        if _is_torch(delta_lin):
+            import torch
+            out = torch.empty(delta_lin.shape, dtype=torch.float32, device=delta_lin.device)
+            check(L.prc_d2z_smooth(self._ctx, _dev_ptr(delta_lin.reshape(-1), "float32", self.n3), 1, int(radius),
+                                   _dev_ptr(out.reshape(-1), "float32", self.n3), 1))
+            return out
+        d = np.ascontiguousarray(delta_lin, np.float32)
+        out = np.empty(d.shape, np.float32)
+        check(L.prc_d2z_smooth(self._ctx, _host_ptr(d, np.float32, self.n3), 0, int(radius),
+                               _host_ptr(out, np.float32, self.n3), 0))
+        return out
+
+    def last_timing(self):
+        ms = (ctypes.c_float * 3)()
+        check(load().prc_d2z_last_timing(self._ctx, ms))
+        return tuple(ms)
+
+    def profile(self, enable: bool = True) -> None:
+        """Per-kernel CUDA-event timing on/off (resets the totals)."""
+        check(load().prc_d2z_profile(self._ctx, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        """{kind: (total ms, launches)} since the last profile() call."""
+        ms = (ctypes.c_double * _lib.PRC_NKINDS)()
+        n = (ctypes.c_longlong * _lib.PRC_NKINDS)()
+        check(load().prc_d2z_profile_read(self._ctx, ms, n))
+        return {k: (ms[i], n[i]) for i, k in enumerate(_lib.KINDS)}
+
+    def last_launches(self) -> int:
+        n = ctypes.c_int()
+        check(load().prc_d2z_last_launches(self._ctx, ctypes.byref(n)))
+        return n.value
+
+    # ---------------------------------------------------------------- history
+    def history(self, zreion):
+        """GetHistory: (counts, history, history_z), each PRC_NHISTORY long."""
+        L = load()
+        counts = np.zeros(PRC_NHISTORY, np.uint32)
+        hist = np.zeros(PRC_NHISTORY, np.float32)
+        hz = np.zeros(PRC_NHISTORY, np.float32)
+        if _is_torch(zreion):
+            zp, on_dev = _dev_ptr(zreion.reshape(-1), "float32", self.n3), 1
+        else:
+            z = np.ascontiguousarray(zreion, np.float32)
+            zp, on_dev = _host_ptr(z, np.float32, self.n3), 0
+        check(L.prc_d2z_history(self._ctx, zp, on_dev, ctypes.c_void_p(counts.ctypes.data),
+                                ctypes.c_void_p(hist.ctypes.data), ctypes.c_void_p(hz.ctypes.data)))
+        return counts, hist, hz
+
+    # ---------------------------------------------------------------- adjoint
+    def backward(self, dL_dz, argmax, dL_ddelta=None, want_dB: bool = True):
+        """(dL/dz, argmax) -> (dL/d delta_lin, dL/dB_r | None)."""
+        L = load()
+        dB = np.zeros(self.n_radii, np.float64) if want_dB else None
+        dBp = ctypes.c_void_p(dB.ctypes.data) if dB is not None else None
+        if _is_torch(dL_dz):
+            import torch
+            gp = _dev_ptr(dL_dz.reshape(-1), "float32", self.n3)
+            ap = _dev_ptr(argmax.reshape(-1), "uint8", self.n3)
+            if dL_ddelta is None:
+                dL_ddelta = torch.empty(dL_dz.shape, dtype=torch.float32, device=dL_dz.device)
+            op = _dev_ptr(dL_ddelta.reshape(-1), "float32", self.n3)
+            check(L.prc_d2z_backward(self._ctx, gp, ap, 1, op, 1, dBp))
+        else:
+            g = np.ascontiguousarray(dL_dz, np.float32)
+            a = np.ascontiguousarray(argmax, np.uint8)
+            if dL_ddelta is None:
+                dL_ddelta = np.empty(g.shape, np.float32)
+            check(L.prc_d2z_backward(self._ctx, _host_ptr(g, np.float32, self.n3),
+                                     _host_ptr(a, np.uint8, self.n3), 0,
+                                     _host_ptr(dL_ddelta, np.float32, self.n3), 0, dBp))
+        return dL_ddelta, dB
+
+
+def delta2zreion(delta_lin, p: Parameters, cl: CLParameters, **kw):
+    """delta_lin -> (zreion, argmax, sigma_grid, tables): main_d2z.C:57-71 in one call."""
+    with Delta2Zreion.from_parameters(p, cl, sigma_grid=True, **kw) as ctx:
+        z, a, s = ctx.forward(delta_lin, want_sigma_grid=True)
+        return z, a, s, ctx.tables

@@ -1,0 +1,91 @@
+"""CPU-only checks of the shared library: it loads, exports every symbol the
+header declares, and validates arguments before touching a device."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import prc_d2z
+from prc_d2z import _lib
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    src = open(os.path.join(REPO, "include", "prc_d2z.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(prc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    names = _header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_lib.EXPORTS)
+
+
+def test_supported_sizes():
+    s = prc_d2z.supported_sizes()
+    for n in (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512, 1024):
+        assert n in s
+    assert 100 not in s
+
+
+def _desc(N=32, nr=4, **kw):
+    R = np.linspace(2.0, 8.0, nr)
+    B = np.full(nr, 5.0)
+    d = _lib.prc_d2z_desc()
+    d.N = N
+    d.n_radii = nr
+    d.box_mpc = 70.0
+    d.radii_mpc = R.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.barrier_b = B.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.barrier_a = 0.75
+    d.growth_init = 1.0
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d, (R, B)
+
+
+@pytest.mark.parametrize("kw,code", [
+    ({"N": 100}, _lib.PRC_ERR_UNSUPPORTED),
+    ({"n_radii": 0}, _lib.PRC_ERR_INVALID),
+    ({"n_radii": 300}, _lib.PRC_ERR_INVALID),
+    ({"box_mpc": 0.0}, _lib.PRC_ERR_INVALID),
+    ({"growth_init": -1.0}, _lib.PRC_ERR_INVALID),
+    ({"barrier_a": 0.0}, _lib.PRC_ERR_INVALID),
+    ({"radius_batch": 99}, _lib.PRC_ERR_INVALID),
+])
+def test_create_rejects_bad_descriptors(kw, code):
+    L = _lib.load()
+    nr = kw.get("n_radii", 4)
+    d, keep = _desc(**{k: v for k, v in kw.items() if k != "n_radii"}, n_radii=nr) if "n_radii" in kw else _desc(**kw)
+    ctx = ctypes.c_void_p()
+    st = L.prc_d2z_create(ctypes.byref(d), ctypes.byref(ctx))
+    assert st == code
+    assert not ctx.value
+    assert len(L.prc_last_error()) > 0
+
+
+def test_null_arguments_are_errors_not_crashes():
+    L = _lib.load()
+    assert L.prc_d2z_create(None, None) == _lib.PRC_ERR_INVALID
+    assert L.prc_d2z_forward(None, None, 0, None, None, 0, None) == _lib.PRC_ERR_INVALID
+    assert L.prc_d2z_history(None, None, 0, None, None, None) == _lib.PRC_ERR_INVALID
+    assert L.prc_d2z_backward(None, None, None, 0, None, 0, None) == _lib.PRC_ERR_INVALID
+    assert L.prc_d2z_destroy(None) == _lib.PRC_OK
+    assert L.prc_compute_tables(None, None) == _lib.PRC_ERR_INVALID
+
+
+def test_python_binding_raises_loudly_without_library(tmp_path):
+    with pytest.raises(RuntimeError, match="missing"):
+        _lib._lib_saved = _lib._lib
+        try:
+            _lib._lib = None
+            _lib.load(str(tmp_path / "nope.so"))
+        finally:
+            _lib._lib = _lib._lib_saved
