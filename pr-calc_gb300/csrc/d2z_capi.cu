@@ -192,30 +192,56 @@ void free_all(prc_d2z_ctx* c) {
   c->pev.clear();
 }
 
-ColSeg seg(const float2* in, float2* out, int rs, int os, int no, int ncp, int tr) {
-  ColSeg s;
+// main-array segment of a column pass along x (rows ix) or y (rows iy)
+TileSeg mseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool xpass) {
+  TileSeg s;
   s.in = in;
   s.out = out;
-  s.row_stride = rs;
-  s.outer_stride = os;
-  s.n_outer = no;
-  s.n_cp = ncp;
-  s.transpose = tr;
+  s.row_stride = xpass ? c->N * c->H : c->H;
+  s.outer_stride = xpass ? c->H : c->N * c->H;
+  s.n_outer = c->N;
+  s.tpo = c->H / c->ksl.tile_w;
+  s.transpose = 0;
+  s.nyq = 0;
+  return s;
+}
+
+// Nyquist-plane segment: rows at stride N, columns contiguous; optionally
+// written transposed
+TileSeg qseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool transpose) {
+  TileSeg s;
+  s.in = in;
+  s.out = out;
+  s.row_stride = c->N;
+  s.outer_stride = 0;
+  s.n_outer = 1;
+  s.tpo = c->N / c->ksl.tile_w;
+  s.transpose = transpose ? 1 : 0;
+  s.nyq = 1;
   return s;
 }
 
 // one column pass over the main array and the Nyquist plane
-void run_col(prc_d2z_ctx* c, bool inv, ColSeg s0, ColSeg s1, int nslots) {
-  ColArgs a;
+void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb = 1, int r0 = 0, int first = 0) {
+  TileArgs a;
+  memset(&a, 0, sizeof(a));
   a.seg[0] = s0;
   a.seg[1] = s1;
   a.slot_stride = c->slot_f2;
   a.tw = c->tw;
-  const int items = s0.n_outer * s0.n_cp + s1.n_outer * s1.n_cp;
-  dim3 grid(grid_for(items, c->ksl.col_groups, c->ksl.occ_col, c->sms), nslots, 1);
+  a.nb = nb;
+  a.first = first;
+  if (mode == TM_WIN || mode == TM_ACC)
+    for (int b = 0; b < nb; ++b) a.kr[b] = c->kr[r0 + b];
+  const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
+  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : c->ksl.occ_tile;
+  dim3 grid(grid_for(tiles, 1, occ, c->sms), gy, 1);
+  const int kind = mode == TM_FWD ? PRC_KIND_COL_FWD
+                 : mode == TM_INV ? PRC_KIND_COL_INV
+                 : mode == TM_WIN ? PRC_KIND_WIN_X : PRC_KIND_ADJ_X;
   {
-    Prof pf(c, inv ? PRC_KIND_COL_INV : PRC_KIND_COL_FWD);
-    c->ks->col(c->ksl, inv, grid, c->st, a);
+    Prof pf(c, kind);
+    c->ks->tile(c->ksl, mode, grid, c->st, a);
   }
   c->launches++;
 }
@@ -246,9 +272,9 @@ void forward_r2c(prc_d2z_ctx* c, const float* d_delta) {
   }
   c->launches++;
   // y pass: main in place; Nyquist Qt[iy][ix] -> Q[ix][ky]
-  run_col(c, false, seg(S, S, H, N * H, N, H / 2, 0), seg(Qt, Q, N, 0, 1, N / 2, 1), 1);
+  run_tile(c, TM_FWD, mseg(c, S, S, false), qseg(c, Qt, Q, true), 1);
   // x pass: main in place; Nyquist Q in place
-  run_col(c, false, seg(S, S, N * H, H, N, H / 2, 0), seg(Q, Q, N, 0, 1, N / 2, 0), 1);
+  run_tile(c, TM_FWD, mseg(c, S, S, true), qseg(c, Q, Q, false), 1);
 }
 
 }  // namespace
@@ -372,7 +398,6 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
     const int nb = (c->nr - r0 < c->B) ? c->nr - r0 : c->B;
     SweepArgs sa;
     memset(&sa, 0, sizeof(sa));
-    sa.spec = c->spec;
     sa.slots = c->slots;
     sa.slot_stride = c->slot_f2;
     sa.tw = c->tw;
@@ -383,17 +408,12 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
     sa.r0 = r0;
     sa.first = (r0 == 0);
     sa.as = c->as;
-    for (int b = 0; b < nb; ++b) {
-      sa.kr[b] = c->kr[r0 + b];
-      sa.cb[b] = c->cb[r0 + b];
-    }
-    {
-      Prof pf(c, PRC_KIND_WIN_X);
-      c->ks->win_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_win, c->sms), c->st, sa);
-    }
-    c->launches++;
+    for (int b = 0; b < nb; ++b) sa.cb[b] = c->cb[r0 + b];
     float2* U = c->slots;
-    run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), nb);
+    // window + inverse x pass: spectrum -> slots (Nyquist plane transposed)
+    run_tile(c, TM_WIN, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1, nb, r0);
+    // inverse y pass of every slot, in place
+    run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), nb);
     {
       Prof pf(c, PRC_KIND_C2R_Z);
       c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, sa);
@@ -452,19 +472,9 @@ int prc_d2z_smooth(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, 
     d_out = c->zre;
   }
   forward_r2c(c, d_delta);
-  SweepArgs sa;
-  memset(&sa, 0, sizeof(sa));
-  sa.spec = c->spec;
-  sa.slots = c->slots;
-  sa.slot_stride = c->slot_f2;
-  sa.tw = c->tw;
-  sa.nb = 1;
-  sa.r0 = radius;
-  sa.kr[0] = c->kr[radius];
-  c->ks->win_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_win, c->sms), c->st, sa);
-  c->launches++;
   float2* U = c->slots;
-  run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), 1);
+  run_tile(c, TM_WIN, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1, 1, radius);
+  run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), 1);
   AdjArgs fa;
   memset(&fa, 0, sizeof(fa));
   fa.slots = U;
@@ -553,30 +563,24 @@ int prc_d2z_backward(prc_d2z_ctx* c, const float* dL_dz, const uint8_t* argmax, 
     aa.A = (float)c->A;
     aa.slots = U;
     aa.slot_stride = c->slot_f2;
-    aa.acc = acc;
     aa.tw = c->tw;
     aa.dB = dL_dB ? c->dB : nullptr;
     aa.nb = nb;
     aa.r0 = r0;
-    aa.first = (r0 == 0);
-    for (int b = 0; b < nb; ++b) aa.kr[b] = c->kr[r0 + b];
     {
       Prof pf(c, PRC_KIND_ADJ_Z);
       c->ks->adj_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_adj_z, c->sms), c->st, aa);
     }
     c->launches++;
     // forward y pass of each slot; Nyquist scratch Qt_b -> Q_b[ix][ky]
-    run_col(c, false, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * (H + 1), U + NN * H, N, 0, 1, N / 2, 1), nb);
-    {
-      Prof pf(c, PRC_KIND_ADJ_X);
-      c->ks->adj_x(c->ksl, grid_for(N * (H / 2) + N / 2, c->ksl.col_groups, c->ksl.occ_adj_x, c->sms), c->st, aa);
-    }
-    c->launches++;
+    run_tile(c, TM_FWD, mseg(c, U, U, false), qseg(c, U + NN * (H + 1), U + NN * H, true), nb);
+    // forward x pass of each slot, acc += W_b * (.)
+    run_tile(c, TM_ACC, mseg(c, U, acc, true), qseg(c, U + NN * H, acc + NN * H, false), 1, nb, r0, r0 == 0);
   }
   PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
   // inverse of the accumulated spectrum into slot 0, then the z C2R
-  run_col(c, true, seg(acc, U, N * H, H, N, H / 2, 0), seg(acc + NN * H, U + NN * H, N, 0, 1, N / 2, 1), 1);
-  run_col(c, true, seg(U, U, H, N * H, N, H / 2, 0), seg(U + NN * H, U + NN * H, N, 0, 1, N / 2, 0), 1);
+  run_tile(c, TM_INV, mseg(c, acc, U, true), qseg(c, acc + NN * H, U + NN * H, true), 1);
+  run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), 1);
   AdjArgs fa;
   memset(&fa, 0, sizeof(fa));
   fa.slots = U;

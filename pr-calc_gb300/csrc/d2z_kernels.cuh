@@ -1,24 +1,25 @@
 // d2z_kernels.cuh — the delta2zreion hot path as sm_103a kernels.
 //
-// Device layout of one box (N = grid side, H = N/2, NN = N*N), in float2 units:
-//   spectrum  : main S[ix][iy][kz] (kz < H, NN*H entries) followed by the
-//               kz = H (Nyquist) plane Q[ix][iy] (NN entries)
-//   slot b    : same size; main U_b[ix][iy][kz], Nyquist plane transposed
-//               Qt_b[iy][ix] so that its y pass is a strided-column pass too
-// A "column pass" transforms along ix or iy: a group of G threads owns two
-// adjacent columns (one 16-byte access per row) and all N rows; adjacent
-// groups own adjacent columns, so a CTA touches whole 128-byte row segments.
-// A "line pass" transforms along z: a group owns one contiguous line and uses
-// the half-length complex FFT of a real sequence (even samples in .x, odd in .y).
+// Device layout of one box (N = grid side, H = N/2, NN = N*N), in float2 units,
+// "slot" size NN*(H+2):
+//   main      [0, NN*H)         X[ix][iy][kz], kz < H
+//   Nyquist   [NN*H, NN*(H+1))  the kz = H plane; Q[ix][iy] in the spectrum,
+//                               transposed Qt[iy][ix] in the radius slots
+//   scratch   [NN*(H+1), NN*(H+2)) a transposed copy for the forward y pass
+// Column passes (along ix or iy) run on tiles of T adjacent columns x N rows:
+// the CTA loads the tile with coalesced 16-byte accesses (a warp covers whole
+// 128-byte row segments) into an XOR-swizzled shared-memory tile, one group of
+// G threads transforms each column in place, and the CTA writes the tile back
+// the same way.  Line passes (along z) give each group one contiguous line and
+// use the half-length complex FFT of a real sequence (even samples in .x,
+// odd in .y).
 //
 // Reference steps fused here (pr-calc c++/src):
-//   k_r2c_z + k_col(fwd, y) + k_col(fwd, x) : main_d2z.C:57-59 (delta /= DInit)
-//                                            and the R2C at main_d2z.C:67
-//   k_win_x   : window loop delta2zreion_d2z.C:57-89 + first axis of the C2R (:92)
-//   k_col(inv): second axis of the C2R
-//   k_c2r_z   : last axis of the C2R, NormalizeArray (:93), GetMeanSigma (:94),
-//               barrier d2z (:206-216) and the running max (:105-146)
-//   k_hist    : GetHistory binning (bubblehistory_d2z.C:17-28)
+//   k_r2c_z + k_tile<FWD> (y, x)  main_d2z.C:57-59 (delta /= DInit) and the R2C (:67)
+//   k_tile<WIN>   window loop delta2zreion_d2z.C:57-89 + first axis of the C2R (:92)
+//   k_tile<INV>   second axis of the C2R
+//   k_c2r_z       last axis of the C2R, NormalizeArray (:93), GetMeanSigma (:94),
+//                 barrier d2z (:206-216) and the running max (:105-146)
 #pragma once
 #include "fft.cuh"
 
@@ -28,60 +29,92 @@ constexpr int kMaxBatch = 16;
 constexpr int kNHistory = 100000;
 
 // ------------------------------------------------------------ per-N plans
-// Column plan: Plan<E, radices...> of length N; line plan: length N/2.
-template <int N> struct Cfg;
-template <> struct Cfg<8> { using Col = Plan<8, 8>; using Line = Plan<4, 4>; };
-template <> struct Cfg<12> { using Col = Plan<12, 4, 3>; using Line = Plan<6, 3, 2>; };
-template <> struct Cfg<16> { using Col = Plan<16, 16>; using Line = Plan<8, 8>; };
-template <> struct Cfg<24> { using Col = Plan<12, 4, 3, 2>; using Line = Plan<12, 4, 3>; };
-template <> struct Cfg<32> { using Col = Plan<16, 16, 2>; using Line = Plan<16, 16>; };
-template <> struct Cfg<48> { using Col = Plan<12, 4, 4, 3>; using Line = Plan<12, 4, 3, 2>; };
-template <> struct Cfg<64> { using Col = Plan<16, 16, 4>; using Line = Plan<8, 8, 4>; };
-template <> struct Cfg<96> { using Col = Plan<24, 8, 4, 3>; using Line = Plan<12, 4, 4, 3>; };
-template <> struct Cfg<128> { using Col = Plan<16, 16, 8>; using Line = Plan<8, 8, 8>; };
-template <> struct Cfg<192> { using Col = Plan<24, 8, 8, 3>; using Line = Plan<24, 8, 4, 3>; };
-template <> struct Cfg<256> { using Col = Plan<16, 16, 16>; using Line = Plan<16, 16, 8>; };
-template <> struct Cfg<512> { using Col = Plan<16, 8, 8, 8>; using Line = Plan<8, 8, 8, 4>; };
-template <> struct Cfg<1024> { using Col = Plan<16, 16, 16, 4>; using Line = Plan<16, 16, 16, 2>; };
+// Line plan (length N/2): Plan<E, radices...>.
+template <int N> struct LCfg;
+template <> struct LCfg<8> { using P = Plan<4, 4>; };
+template <> struct LCfg<12> { using P = Plan<6, 3, 2>; };
+template <> struct LCfg<16> { using P = Plan<8, 8>; };
+template <> struct LCfg<24> { using P = Plan<12, 4, 3>; };
+template <> struct LCfg<32> { using P = Plan<8, 8, 2>; };
+template <> struct LCfg<48> { using P = Plan<12, 4, 3, 2>; };
+template <> struct LCfg<64> { using P = Plan<8, 8, 4>; };
+template <> struct LCfg<96> { using P = Plan<12, 4, 4, 3>; };
+template <> struct LCfg<128> { using P = Plan<8, 8, 8>; };
+template <> struct LCfg<192> { using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct LCfg<256> { using P = Plan<8, 8, 4, 4>; };
+template <> struct LCfg<512> { using P = Plan<8, 8, 8, 4>; };
+template <> struct LCfg<1024> { using P = Plan<8, 8, 8, 8>; };
 
+// Tile plan (length N), tile width T (columns; T divides N/2 and N) and the
+// two shifts (SA, SB) of the tile swizzle (chosen by simulating the bank
+// pattern of every shared-memory access of the plan; SB = 0: unused).
+template <int N> struct TCfg;
+template <> struct TCfg<8> { using P = Plan<8, 8>; static constexpr int T = 4, SA = 1, SB = 0; };
+template <> struct TCfg<12> { using P = Plan<12, 4, 3>; static constexpr int T = 6, SA = 1, SB = 0; };
+template <> struct TCfg<16> { using P = Plan<8, 8, 2>; static constexpr int T = 8, SA = 1, SB = 0; };
+template <> struct TCfg<24> { using P = Plan<12, 4, 3, 2>; static constexpr int T = 12, SA = 1, SB = 0; };
+template <> struct TCfg<32> { using P = Plan<16, 16, 2>; static constexpr int T = 16, SA = 1, SB = 0; };
+template <> struct TCfg<48> { using P = Plan<12, 4, 4, 3>; static constexpr int T = 8, SA = 1, SB = 0; };
+template <> struct TCfg<64> { using P = Plan<8, 8, 8>; static constexpr int T = 16, SA = 1, SB = 2; };
+template <> struct TCfg<96> { using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16, SA = 1, SB = 0; };
+template <> struct TCfg<128> { using P = Plan<8, 8, 4, 4>; static constexpr int T = 16, SA = 2, SB = 3; };
+template <> struct TCfg<192> { using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, SA = 1, SB = 2; };
+template <> struct TCfg<256> { using P = Plan<16, 16, 16>; static constexpr int T = 16, SA = 1, SB = 4; };
+template <> struct TCfg<512> { using P = Plan<16, 8, 8, 8>; static constexpr int T = 8, SA = 1, SB = 3; };
+template <> struct TCfg<1024> { using P = Plan<16, 16, 16, 4>; static constexpr int T = 4, SA = 1, SB = 2; };
 
-template <int N> struct K {
+template <int N> struct LK {
   static constexpr int H = N / 2;
-  using ColP = typename Cfg<N>::Col;
-  using LineP = typename Cfg<N>::Line;
-  static constexpr int CE = ColP::E;
-  static constexpr int CG = N / CE;
-  static constexpr int LE = LineP::E;
-  static constexpr int LG = H / LE;
-  static_assert(PlanRun<ColP>::L == N, "column plan length");
-  static_assert(PlanRun<LineP>::L == H, "line plan length");
-  static constexpr int COL_THREADS = 256;
-  static constexpr int LINE_THREADS = 256;
-  static constexpr int CNG = COL_THREADS / CG;   // column groups per CTA
-  static constexpr int LNG = LINE_THREADS / LG;  // line groups per CTA
-  static constexpr int col_smem_f2 = N + CNG * GroupBuf<N, 2>::size;
-  static constexpr int line_smem_f2 = N + LNG * GroupBuf<H, 1>::size;
+  using P = typename LCfg<N>::P;
+  static constexpr int E = P::E;
+  static constexpr int G = H / E;
+  static_assert(PlanRun<P>::L == H, "line plan length");
+  static constexpr int THREADS = 256;
+  static constexpr int MINB = E <= 8 ? 3 : 2;  // resident CTAs per SM the register budget is sized for
+  static constexpr int NG = THREADS / G;
+  static constexpr int gsize = GroupBuf<H, G>::size;
+  static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
+  static constexpr int smem_f2 = N + TW + NG * gsize;   // N-table, stage twiddles, group buffers
+};
+
+template <int N> struct TK {
+  static constexpr int H = N / 2;
+  using P = typename TCfg<N>::P;
+  static constexpr int T = TCfg<N>::T;
+  static constexpr int E = P::E;
+  static constexpr int G = N / E;
+  static_assert(PlanRun<P>::L == N, "tile plan length");
+  static_assert(H % T == 0 && N % T == 0 && T % 2 == 0, "tile width");
+  static constexpr int THREADS = T * G;
+  static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
+  static constexpr int smem_f2 = TW + N * T;
+  // resident CTAs per SM the register budget is sized for; the accumulate
+  // mode keeps E more complex values per thread
+  static constexpr int MINB = THREADS >= 512 ? 2 : (THREADS >= 256 ? 3 : 4);
+  static constexpr int MINB_ACC = MINB > 1 ? MINB - 1 : 1;
 };
 
 // ------------------------------------------------------------ kernel args
-struct ColSeg {
+struct TileSeg {
   const float2* in;
   float2* out;
-  int row_stride;    // float2 between FFT rows
+  int row_stride;    // float2 between rows (the transform axis)
   int outer_stride;  // float2 between outer indices
   int n_outer;
-  int n_cp;          // column pairs per outer index
-  int transpose;     // 1: out[(col)*N + row] (a square N x N plane)
+  int tpo;           // tiles per outer index
+  int transpose;     // 1: out[(column)*N + row] (N x N plane)
+  int nyq;           // 1: the kz = H plane (window frequencies: fy = column, fz = H)
 };
 
-struct ColArgs {
-  ColSeg seg[2];            // main + Nyquist plane
-  long long slot_stride;    // float2 between slots (blockIdx.y)
-  const float2* tw;         // N-entry table e^{+2 pi i k/N}
+struct TileArgs {
+  TileSeg seg[2];          // main array, Nyquist plane
+  long long slot_stride;   // plain: per blockIdx.y; WIN: per radius (out); ACC: per radius (in)
+  const float2* tw;        // N-entry table e^{+2 pi i k/N}
+  int nb, first;
+  float kr[kMaxBatch];     // dk * R_b
 };
 
 struct SweepArgs {
-  const float2* spec;   // spectrum (k_win_x input)
   float2* slots;        // slot 0 base
   long long slot_stride;
   const float2* tw;
@@ -92,9 +125,10 @@ struct SweepArgs {
   int r0;               // global index of the first radius
   int first;            // first sweep: zreion/argmax not read
   float as;             // A / N^3
-  float kr[kMaxBatch];  // dk * R_b
   float cb[kMaxBatch];  // A*B_b - 1 (NaN: never wins)
 };
+
+enum TileMode { TM_FWD = 0, TM_INV = 1, TM_WIN = 2, TM_ACC = 3 };
 
 // ------------------------------------------------------------ helpers
 __device__ __forceinline__ int fsq(int f, int n) {
@@ -102,9 +136,11 @@ __device__ __forceinline__ int fsq(int f, int n) {
   return a * a;
 }
 
-// Top-hat window W(x) = 3 (sin x - x cos x) / x^3 (delta2zreion_d2z.C:77),
-// evaluated without the cancellation of the closed form for x < 1 by its
-// Taylor series  sum_m 3 (-1)^m (2m+2) x^{2m} / (2m+3)!.
+// Top-hat window W(x) = 3 (sin x - x cos x) / x^3 (delta2zreion_d2z.C:77).
+// x < 1: the Taylor series sum_m 3 (-1)^m (2m+2) x^{2m} / (2m+3)! (no
+// cancellation).  x >= 1: Cody-Waite reduction of x by 2 pi = C1 + C2 (C1 the
+// float nearest 2 pi; the first FMA is exact for x < 2^10 * 2 pi) to [-pi, pi],
+// then the SFU sine/cosine (absolute error < 2^-21 there).
 __device__ __forceinline__ float tophat(float x) {
   if (x < 1.0f) {
     const float x2 = x * x;
@@ -117,180 +153,254 @@ __device__ __forceinline__ float tophat(float x) {
     p = fmaf(p, x2, 1.0f);
     return p;
   }
-  float s, c;
-  sincosf(x, &s, &c);
-  const float r = 1.0f / x;
-  return 3.0f * fmaf(-x, c, s) * (r * r * r);
+  const float k = rintf(x * 0.159154943091895336f);
+  float r = fmaf(-k, 6.28318548202514648f, x);
+  r = fmaf(-k, -1.74845560e-07f, r);
+  const float s = __sinf(r), c = __cosf(r);
+  const float ix = __frcp_rn(x);
+  return 3.0f * fmaf(-x, c, s) * (ix * ix * ix);
+}
+
+__device__ __forceinline__ float window_of(int m2, float kr) {
+  return (m2 == 0) ? 0.f : tophat(sqrtf((float)m2) * kr);
 }
 
 __device__ __forceinline__ void load_tw(float2* tw_s, const float2* tw, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw_s[i] = tw[i];
-  __syncthreads();
 }
 
-// ============================================================ column pass
-// Generic strided pass without window: F2/F3 (forward) and P2 (inverse).
-template <int N, bool INV>
-__global__ void __launch_bounds__(K<N>::COL_THREADS, 2) k_col(ColArgs a) {
-  using KK = K<N>;
-  constexpr int E = KK::CE, G = KK::CG, NG = KK::CNG;
-  extern __shared__ float4 smem4[];
-  float2* tw = reinterpret_cast<float2*>(smem4);
-  load_tw(tw, a.tw, N);
-  const int g = threadIdx.x / G, t = threadIdx.x % G;
-  float2* gbuf = tw + N + g * GroupBuf<N, 2>::size;
-  GroupSync<G> sync(g);
-  const long long soff = (long long)blockIdx.y * a.slot_stride;
-  const int items0 = a.seg[0].n_outer * a.seg[0].n_cp;
-  const int items = items0 + a.seg[1].n_outer * a.seg[1].n_cp;
-  for (int s = blockIdx.x; s * NG < items; s += gridDim.x) {
-    const int item = s * NG + g;
-    const bool valid = item < items;
-    const bool si = item >= items0;
-    // field-wise select keeps the segment descriptors in the parameter bank
-    const int n_cp = si ? a.seg[1].n_cp : a.seg[0].n_cp;
-    const int row_stride = si ? a.seg[1].row_stride : a.seg[0].row_stride;
-    const int outer_stride = si ? a.seg[1].outer_stride : a.seg[0].outer_stride;
-    const int transpose = si ? a.seg[1].transpose : a.seg[0].transpose;
-    const float2* sin_ = si ? a.seg[1].in : a.seg[0].in;
-    float2* sout = si ? a.seg[1].out : a.seg[0].out;
-    const int it = valid ? (si ? item - items0 : item) : 0;
-    const int outer = it / n_cp;
-    const int cpi = it - outer * n_cp;
-    const float2* in = sin_ + soff + (long long)outer * outer_stride + 2 * cpi;
-    float2 v[2][E];
+// Copies a per-radius parameter array into shared memory with compile-time
+// indices (a runtime index into kernel parameters would force a local copy);
+// thread 0 does it, so it works for CTAs of any size.
+__device__ __forceinline__ void stage_params(float* dst, const float (&src)[kMaxBatch]) {
+  if (threadIdx.x == 0) {
 #pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int row = t + G * m;
-      float4 q = valid ? __ldg(reinterpret_cast<const float4*>(in + (long long)row * row_stride))
-                       : make_float4(0.f, 0.f, 0.f, 0.f);
-      v[0][m] = make_float2(q.x, q.y);
-      v[1][m] = make_float2(q.z, q.w);
-    }
-    PlanRun<typename KK::ColP>::template run<2, INV, 1>(v, gbuf, t, tw, sync);
-    if (valid) {
-      float2* out = sout + soff;
-      if (!transpose) {
-        out += (long long)outer * outer_stride + 2 * cpi;
-#pragma unroll
-        for (int m = 0; m < E; ++m) {
-          const int row = t + G * m;
-          reinterpret_cast<float4*>(out + (long long)row * row_stride)[0] =
-              make_float4(v[0][m].x, v[0][m].y, v[1][m].x, v[1][m].y);
-        }
-      } else {
-#pragma unroll
-        for (int m = 0; m < E; ++m) {
-          const int row = t + G * m;
-          out[(2 * cpi) * N + row] = v[0][m];
-          out[(2 * cpi + 1) * N + row] = v[1][m];
-        }
-      }
-    }
+    for (int i = 0; i < kMaxBatch; ++i) dst[i] = src[i];
   }
 }
 
-// ============================================================ window + x pass
-// For each radius of the sweep: delta_hat * W(|k| R_b) (k = 0 -> 0), inverse
-// FFT along x, into slot b.  The spectrum tile is re-read per radius (L1/L2).
-template <int N>
-__global__ void __launch_bounds__(K<N>::COL_THREADS, 2) k_win_x(SweepArgs a) {
-  using KK = K<N>;
-  constexpr int H = N / 2, E = KK::CE, G = KK::CG, NG = KK::CNG;
-  constexpr long long NN = (long long)N * N;
-  extern __shared__ float4 smem4[];
-  float2* tw = reinterpret_cast<float2*>(smem4);
-  load_tw(tw, a.tw, N);
-  const int g = threadIdx.x / G, t = threadIdx.x % G;
-  float2* gbuf = tw + N + g * GroupBuf<N, 2>::size;
-  GroupSync<G> sync(g);
-  const int items0 = N * (H / 2);
-  const int items = items0 + N / 2;
-  for (int s = blockIdx.x; s * NG < items; s += gridDim.x) {
-    const int item = s * NG + g;
-    const bool valid = item < items;
-    const bool nyq = item >= items0;
-    // source pointer, row stride, and squared frequency of the two columns
-    const float2* in;
-    int row_stride, syz0, syz1, c0;
-    if (!nyq) {
-      const int it = valid ? item : 0;
-      const int iy = it / (H / 2), cp = it % (H / 2);
-      in = a.spec + (long long)iy * H + 2 * cp;
-      row_stride = N * H;
-      const int fy2 = fsq(iy, N);
-      syz0 = fy2 + (2 * cp) * (2 * cp);
-      syz1 = fy2 + (2 * cp + 1) * (2 * cp + 1);
-      c0 = 2 * cp;
+// ------------------------------------------------------------ tiles
+// A T-column tile is cut into 128-byte lines of 16 float2 words (16/T rows
+// each); word w of line l is stored at l*16 + (w ^ f(l)),
+// f(l) = (l ^ (l >> SA) ^ (l >> SB)) & 15.  With the per-N shifts of TCfg no
+// access of the plan (group column reads, every Stockham store, the
+// cooperative row loads) puts two lanes of a half-warp on one bank pair.
+// Tiles whose width is not a power of two are not swizzled.
+template <int N> struct TileSw {
+  static constexpr int T = TCfg<N>::T, SA = TCfg<N>::SA, SB = TCfg<N>::SB;
+  static constexpr bool on = IsPow2<T>::v && T <= 16;
+  static constexpr int RPL = on ? 16 / T : 1;  // rows per line
+  static __device__ __forceinline__ constexpr int f(int l) {
+    return (l ^ (l >> SA) ^ (SB ? (l >> SB) : 0)) & 15;
+  }
+  static __device__ __forceinline__ int idx(int p, int c) {
+    if constexpr (!on) {
+      return p * T + c;
     } else {
-      const int cp = item - items0;
-      in = a.spec + NN * H + 2 * cp;
-      row_stride = N;
-      syz0 = fsq(2 * cp, N) + H * H;
-      syz1 = fsq(2 * cp + 1, N) + H * H;
-      c0 = 2 * cp;
+      const int l = p / RPL;
+      return l * 16 + (((p % RPL) * T + c) ^ f(l));
     }
-    int sx[E];
+  }
+};
+
+// One column of a tile.  The swizzle is linear over GF(2), so for a row
+// tp | cp (disjoint thread bits tp and compile-time bits cp) the index is
+// (h ^ D(cp)) + 16 * (cp / RPL), h = thread(tp): one XOR per access.
+template <int N> struct TileCol {
+  using S = TileSw<N>;
+  float2* tile;
+  int col;
+  __device__ __forceinline__ int thread(int tp) const {
+    if constexpr (S::on)
+      return 16 * (tp / S::RPL) | (col ^ ((tp % S::RPL) * S::T) ^ S::f(tp / S::RPL));
+    else
+      return tp * S::T + col;
+  }
+  static __device__ __forceinline__ int off(int h, int cp) {
+    if constexpr (S::on)
+      return (h ^ (((cp % S::RPL) * S::T) ^ S::f(cp / S::RPL))) + 16 * (cp / S::RPL);
+    else
+      return h + cp * S::T;
+  }
+  __device__ __forceinline__ float2 get(int h, int cp) const { return tile[off(h, cp)]; }
+  __device__ __forceinline__ void put(int h, int cp, float2 v) const { tile[off(h, cp)] = v; }
+  __device__ __forceinline__ float2 get_pos(int p) const { return tile[S::idx(p, col)]; }
+  __device__ __forceinline__ void put_pos(int p, float2 v) const { tile[S::idx(p, col)] = v; }
+};
+
+// Cooperative tile traffic: 16-byte chunks (two columns), consecutive threads
+// along a row, a warp covering whole row segments.  Thread rows are tp =
+// tid / CPR, iteration i adds the constant row i * RPI.
+template <int N, int THREADS> struct TileIO {
+  static constexpr int T = TCfg<N>::T, CPR = T / 2, RPI = THREADS / CPR, ITER = N / RPI;
+  static_assert(THREADS % CPR == 0 && N % RPI == 0, "tile io shape");
+  const int tp, cc;
+  TileCol<N> c0, c1;
+  int h0, h1;
+  __device__ __forceinline__ TileIO(float2* tile)
+      : tp(threadIdx.x / CPR), cc(threadIdx.x % CPR), c0{tile, 2 * (threadIdx.x % CPR)},
+        c1{tile, 2 * (threadIdx.x % CPR) + 1} {
+    h0 = c0.thread(tp);
+    h1 = c1.thread(tp);
+  }
+  __device__ __forceinline__ void load(const float2* base, int row_stride) const {
+    const float2* src = base + (long long)tp * row_stride + 2 * cc;
+    const long long step = (long long)RPI * row_stride;
 #pragma unroll
-    for (int m = 0; m < E; ++m) sx[m] = fsq(t + G * m, N);
-    for (int b = 0; b < a.nb; ++b) {
-      const float kr = a.kr[b];
-      float2 v[2][E];
+    for (int i = 0; i < ITER; ++i) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(src + i * step));
+      c0.put(h0, i * RPI, make_float2(v.x, v.y));
+      c1.put(h1, i * RPI, make_float2(v.z, v.w));
+    }
+  }
+  __device__ __forceinline__ void store(float2* base, int row_stride) const {
+    float2* dst = base + (long long)tp * row_stride + 2 * cc;
+    const long long step = (long long)RPI * row_stride;
 #pragma unroll
-      for (int m = 0; m < E; ++m) {
-        const int row = t + G * m;
-        float4 q = valid ? __ldg(reinterpret_cast<const float4*>(in + (long long)row * row_stride))
-                         : make_float4(0.f, 0.f, 0.f, 0.f);
-        v[0][m] = make_float2(q.x, q.y);
-        v[1][m] = make_float2(q.z, q.w);
-      }
-      // window: rows ix and N-ix share |k|, so each pair is evaluated once
+    for (int i = 0; i < ITER; ++i) {
+      const float2 a = c0.get(h0, i * RPI), b = c1.get(h1, i * RPI);
+      *reinterpret_cast<float4*>(dst + i * step) = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+  // base += tile (base = 0 first if zero)
+  __device__ __forceinline__ void accumulate(float2* base, int row_stride, bool zero) const {
+    float2* dst = base + (long long)tp * row_stride + 2 * cc;
+    const long long step = (long long)RPI * row_stride;
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int syz = c ? syz1 : syz0;
-        float w[E];
+    for (int i = 0; i < ITER; ++i) {
+      const float2 a = c0.get(h0, i * RPI), b = c1.get(h1, i * RPI);
+      float4* d = reinterpret_cast<float4*>(dst + i * step);
+      float4 o = zero ? make_float4(0.f, 0.f, 0.f, 0.f) : *d;
+      o.x += a.x;
+      o.y += a.y;
+      o.z += b.x;
+      o.w += b.y;
+      *d = o;
+    }
+  }
+};
+
+// Transposed store of an N x N plane tile: column c -> out[(c0 + c)*N + row].
+template <int N, int T, int THREADS>
+__device__ __forceinline__ void tile_store_t(const float2* tile, float2* out, int c0) {
+  constexpr int CPC = N / 2;  // chunks per column
+  for (int q = threadIdx.x; q < T * CPC; q += THREADS) {
+    const int c = q / CPC, pp = q - (q / CPC) * CPC;
+    const float2 a = tile[TileSw<N>::idx(2 * pp, c)], b = tile[TileSw<N>::idx(2 * pp + 1, c)];
+    *reinterpret_cast<float4*>(out + (long long)(c0 + c) * N + 2 * pp) = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+// ============================================================ column pass
+// One kernel for every column pass:
+//   TM_FWD / TM_INV  plain forward / inverse transform, in -> out (blockIdx.y
+//                    selects a slot), same layout or transposed;
+//   TM_WIN           per radius b: spectrum * W_b (k = 0 -> 0), inverse, -> slot b;
+//   TM_ACC           per radius b: forward transform of slot b, acc += W_b * (.).
+// Rows ix and N-ix share |k|, so in the window modes each pair of rows is
+// evaluated once and handed to the mirror lane by a shuffle.
+template <int N, int MODE>
+__global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_ACC : TK<N>::MINB)
+    k_tile(TileArgs a) {
+  using KK = TK<N>;
+  constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, TH = KK::THREADS;
+  constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);
+  constexpr bool WIN = (MODE == TM_WIN || MODE == TM_ACC);
+  extern __shared__ float4 smem4[];
+  float2* tws = reinterpret_cast<float2*>(smem4);  // stage twiddles
+  float2* tile = tws + KK::TW;
+  __shared__ float s_kr[kMaxBatch];
+  if constexpr (WIN) stage_params(s_kr, a.kr);
+  PlanRun<typename KK::P>::template fill<1>(tws, a.tw);
+  __syncthreads();
+  const int g = threadIdx.x / G, t = threadIdx.x - (threadIdx.x / G) * G;
+  // CTAs smaller than a warp (the smallest grids) name only their own lanes
+  constexpr unsigned LANES = TH >= 32 ? 0xffffffffu : ((1u << TH) - 1u);
+  GroupSync<G> sync(g, LANES);
+  const TileCol<N> col{tile, g};
+  const TileIO<N, TH> io(tile);
+  constexpr bool SPLIT = PlanRun<typename KK::P>::SPLIT;
+  const int hrow = col.thread(t);  // rows t + G*m of this group's column
+  const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
+  const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;
+  const int tiles = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;
+  for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+    const bool sn = ti >= tiles0;
+    const TileSeg sg = sn ? a.seg[1] : a.seg[0];
+    const int tl = sn ? ti - tiles0 : ti;
+    const int outer = tl / sg.tpo, tc = tl - (tl / sg.tpo) * sg.tpo;
+    const long long off = (long long)outer * sg.outer_stride + (long long)tc * T;
+    // squared frequency of this group's column, without the row part
+    int syz = 0;
+    if constexpr (WIN) {
+      const int c = tc * T + g;
+      syz = sg.nyq ? fsq(c, N) + H * H : fsq(outer, N) + c * c;
+    }
+    const int nrad = WIN ? a.nb : 1;
+    float2 acc[E];
+    if constexpr (MODE == TM_ACC) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
+    }
+    for (int b = 0; b < nrad; ++b) {
+      const float2* src = sg.in + off + yoff + (MODE == TM_ACC ? (long long)b * a.slot_stride : 0);
+      io.load(src, sg.row_stride);
+      __syncthreads();
+      float2 v[E];
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = SPLIT ? col.get(hrow, G * m) : col.get_pos(t + G * m);
+      float w[E];
+      if constexpr (WIN) {
+        const float kr = s_kr[b];
         constexpr int EH = E / 2;
         constexpr bool share = (G <= 32);
 #pragma unroll
-        for (int m = 0; m < E; ++m) {
-          if (!share || m <= EH) {
-            const int m2 = sx[m] + syz;
-            w[m] = (m2 == 0) ? 0.f : tophat(sqrtf((float)m2) * kr);
-          }
-        }
+        for (int m = 0; m < E; ++m)
+          if (!share || m <= EH) w[m] = window_of(fsq(t + G * m, N) + syz, kr);
         if constexpr (share) {
 #pragma unroll
           for (int m = EH + 1; m < E; ++m) {
-            const float o = __shfl_sync(0xffffffffu, w[E - 1 - m], (G - t) & (G - 1), G);
+            const float o = __shfl_sync(LANES, w[E - 1 - m], (G - t) & (G - 1), G);
             w[m] = (t == 0) ? w[E - m] : o;
           }
-          // m == EH: for t > 0 the directly computed value equals the mirror's
-        }
-#pragma unroll
-        for (int m = 0; m < E; ++m) v[c][m] = cscale(v[c][m], w[m]);
-      }
-      PlanRun<typename KK::ColP>::template run<2, true, 1>(v, gbuf, t, tw, sync);
-      if (valid) {
-        float2* out = a.slots + (long long)b * a.slot_stride;
-        if (!nyq) {
-          const int iy = item / (H / 2), cp = item % (H / 2);
-          out += (long long)iy * H + 2 * cp;
-#pragma unroll
-          for (int m = 0; m < E; ++m) {
-            const int row = t + G * m;
-            reinterpret_cast<float4*>(out + (long long)row * (N * H))[0] =
-                make_float4(v[0][m].x, v[0][m].y, v[1][m].x, v[1][m].y);
-          }
-        } else {
-          out += NN * H;
-#pragma unroll
-          for (int m = 0; m < E; ++m) {
-            const int row = t + G * m;
-            out[(long long)c0 * N + row] = v[0][m];
-            out[(long long)(c0 + 1) * N + row] = v[1][m];
-          }
         }
       }
+      if constexpr (MODE == TM_WIN) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) v[m] = cscale(v[m], w[m]);
+      }
+      PlanRun<typename KK::P>::template run<INV>(v, col, t, tws, sync);
+      if constexpr (MODE == TM_ACC) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          acc[m].x = fmaf(w[m], v[m].x, acc[m].x);
+          acc[m].y = fmaf(w[m], v[m].y, acc[m].y);
+        }
+        __syncthreads();  // the next radius reloads the tile
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          if constexpr (SPLIT) col.put(hrow, G * m, v[m]);
+          else col.put_pos(t + G * m, v[m]);
+        }
+        __syncthreads();
+        float2* dst = sg.out + yoff + (MODE == TM_WIN ? (long long)b * a.slot_stride : 0);
+        if (sg.transpose)
+          tile_store_t<N, T, TH>(tile, dst + (long long)outer * sg.outer_stride, tc * T);
+        else
+          io.store(dst + off, sg.row_stride);
+        __syncthreads();
+      }
+    }
+    if constexpr (MODE == TM_ACC) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        if constexpr (SPLIT) col.put(hrow, G * m, acc[m]);
+        else col.put_pos(t + G * m, acc[m]);
+      }
+      __syncthreads();
+      io.accumulate(sg.out + off, sg.row_stride, a.first != 0);
+      __syncthreads();
     }
   }
 }
@@ -300,26 +410,32 @@ __global__ void __launch_bounds__(K<N>::COL_THREADS, 2) k_win_x(SweepArgs a) {
 // p = t + G*m.  Out: v[m] = X[k] at k = t + G*m (k < H); returns X[H] (real) in
 // lane t == 0.  Z = DFT_H(x_even + i x_odd); X[k] = Ze[k] + e^{-2 pi i k/N} Zo[k].
 template <int N, class Sync>
-__device__ __forceinline__ float line_r2c(float2 (&v)[1][K<N>::LE], float2* gbuf, int t,
-                                          const float2* tw, const Sync& sync) {
-  constexpr int H = N / 2, E = K<N>::LE, G = K<N>::LG;
-  PlanRun<typename K<N>::LineP>::template run<1, false, 2>(v, gbuf, t, tw, sync);
+__device__ __forceinline__ float line_r2c(float2 (&v)[LK<N>::E], float2* gbuf, int t, const float2* tw,
+                                          const float2* tws, const Sync& sync) {
+  constexpr int H = N / 2, E = LK<N>::E, G = LK<N>::G;
+  using P = typename LK<N>::P;
+  const LineBuf<H> buf{gbuf};
+  PlanRun<P>::template run<false>(v, buf, t, tws, sync);
+  const int h = buf.thread(t);
 #pragma unroll
-  for (int m = 0; m < E; ++m) gbuf[Swz<H, 1>::f(t + G * m)] = v[0][m];
+  for (int m = 0; m < E; ++m) {
+    if constexpr (PlanRun<P>::SPLIT) buf.put(h, G * m, v[m]);
+    else buf.put_pos(t + G * m, v[m]);
+  }
   sync();
   float2 p[E];
 #pragma unroll
-  for (int m = 0; m < E; ++m) p[m] = gbuf[Swz<H, 1>::f((H - (t + G * m)) % H)];
+  for (int m = 0; m < E; ++m) p[m] = buf.get_pos((H - (t + G * m)) % H);
   sync();
   float xh = 0.f;
 #pragma unroll
   for (int m = 0; m < E; ++m) {
     const int k = t + G * m;
-    const float2 z = v[0][m], zc = cconj(p[m]);
+    const float2 z = v[m], zc = cconj(p[m]);
     const float2 ze = cscale(cadd(z, zc), 0.5f);
     const float2 d = csub(z, zc);
     const float2 zo = make_float2(0.5f * d.y, -0.5f * d.x);  // d / (2i)
-    v[0][m] = cadd(ze, cmul(cconj(tw[k]), zo));
+    v[m] = cadd(ze, cmul(cconj(tw[k]), zo));
     if (m == 0) xh = ze.x - zo.x;
   }
   return xh;
@@ -330,20 +446,26 @@ __device__ __forceinline__ float line_r2c(float2 (&v)[1][K<N>::LE], float2* gbuf
 // X[H] (read by lane t == 0 only).  Out: v[m] = (x[2p], x[2p+1]) at p = t + G*m,
 // unnormalised.
 template <int N, class Sync>
-__device__ __forceinline__ void line_c2r(float2 (&v)[1][K<N>::LE], float2 xh, float2* gbuf, int t,
-                                         const float2* tw, const Sync& sync) {
-  constexpr int H = N / 2, E = K<N>::LE, G = K<N>::LG;
+__device__ __forceinline__ void line_c2r(float2 (&v)[LK<N>::E], float2 xh, float2* gbuf, int t,
+                                         const float2* tw, const float2* tws, const Sync& sync) {
+  constexpr int H = N / 2, E = LK<N>::E, G = LK<N>::G;
+  using P = typename LK<N>::P;
+  const LineBuf<H> buf{gbuf};
+  const int h = buf.thread(t);
 #pragma unroll
-  for (int m = 0; m < E; ++m) gbuf[Swz<H, 1>::f(t + G * m)] = v[0][m];
+  for (int m = 0; m < E; ++m) {
+    if constexpr (PlanRun<P>::SPLIT) buf.put(h, G * m, v[m]);
+    else buf.put_pos(t + G * m, v[m]);
+  }
   sync();
   float2 p[E];
 #pragma unroll
-  for (int m = 0; m < E; ++m) p[m] = gbuf[Swz<H, 1>::f((H - (t + G * m)) % H)];
+  for (int m = 0; m < E; ++m) p[m] = buf.get_pos((H - (t + G * m)) % H);
   sync();
 #pragma unroll
   for (int m = 0; m < E; ++m) {
     const int k = t + G * m;
-    float2 x = v[0][m], xp = p[m];
+    float2 x = v[m], xp = p[m];
     if (k == 0) {
       x = make_float2(x.x, 0.f);
       xp = make_float2(xh.x, 0.f);
@@ -351,42 +473,44 @@ __device__ __forceinline__ void line_c2r(float2 (&v)[1][K<N>::LE], float2 xh, fl
     const float2 xc = cconj(xp);
     const float2 xe = cadd(x, xc);
     const float2 xo = cmul(csub(x, xc), tw[k]);
-    v[0][m] = make_float2(xe.x - xo.y, xe.y + xo.x);  // xe + i*xo
+    v[m] = make_float2(xe.x - xo.y, xe.y + xo.x);  // xe + i*xo
   }
-  PlanRun<typename K<N>::LineP>::template run<1, true, 2>(v, gbuf, t, tw, sync);
+  PlanRun<P>::template run<true>(v, buf, t, tws, sync);
 }
 
 // ============================================================ forward z pass
-// Real line (N samples, scaled by 1/DInit) -> X[0..H-1] into S and X[H] into
-// the transposed Nyquist plane Qt[iy][ix].
+// Real line (N samples, divided by DInit) -> X[0..H-1] into S and X[H] into
+// the transposed Nyquist scratch Qt[iy][ix].
 template <int N>
-__global__ void __launch_bounds__(K<N>::LINE_THREADS) k_r2c_z(const float* __restrict__ delta,
-                                                               float dinit, float2* S, float2* Qt,
-                                                               const float2* twg) {
-  using KK = K<N>;
-  constexpr int H = N / 2, E = KK::LE, G = KK::LG, NG = KK::LNG;
+__global__ void __launch_bounds__(LK<N>::THREADS, LK<N>::MINB) k_r2c_z(const float* __restrict__ delta, float dinit,
+                                                             float2* S, float2* Qt, const float2* twg) {
+  using KK = LK<N>;
+  constexpr int H = N / 2, E = KK::E, G = KK::G, NG = KK::NG;
   extern __shared__ float4 smem4[];
   float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* tws = tw + N;
   load_tw(tw, twg, N);
+  PlanRun<typename KK::P>::template fill<2>(tws, twg);
+  __syncthreads();
   const int g = threadIdx.x / G, t = threadIdx.x % G;
-  float2* gbuf = tw + N + g * GroupBuf<H, 1>::size;
+  float2* gbuf = tws + KK::TW + g * KK::gsize;
   GroupSync<G> sync(g);
   const int lines = N * N;
   for (int s = blockIdx.x; s * NG < lines; s += gridDim.x) {
     const int l = s * NG + g;
     const bool valid = l < lines;
-    float2 v[1][E];
+    float2 v[E];
     const float2* src = reinterpret_cast<const float2*>(delta + (long long)(valid ? l : 0) * N);
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       float2 q = valid ? __ldg(src + t + G * m) : make_float2(0.f, 0.f);
-      v[0][m] = make_float2(__fdiv_rn(q.x, dinit), __fdiv_rn(q.y, dinit));
+      v[m] = make_float2(__fdiv_rn(q.x, dinit), __fdiv_rn(q.y, dinit));
     }
-    const float xh = line_r2c<N>(v, gbuf, t, tw, sync);
+    const float xh = line_r2c<N>(v, gbuf, t, tw, tws, sync);
     if (valid) {
       float2* dst = S + (long long)l * H;
 #pragma unroll
-      for (int m = 0; m < E; ++m) dst[t + G * m] = v[0][m];
+      for (int m = 0; m < E; ++m) dst[t + G * m] = v[m];
       if (t == 0) {
         const int ix = l / N, iy = l - (l / N) * N;
         Qt[(long long)iy * N + ix] = make_float2(xh, 0.f);
@@ -399,97 +523,85 @@ __global__ void __launch_bounds__(K<N>::LINE_THREADS) k_r2c_z(const float* __res
 // For each radius of the sweep: X[0..H] -> real line, z = A/N^3 * x + (A B_b - 1),
 // running max / argmax in registers, optional sum of x^2; one zreion RMW per sweep.
 template <int N>
-__global__ void __launch_bounds__(K<N>::LINE_THREADS) k_c2r_z(SweepArgs a) {
-  using KK = K<N>;
-  constexpr int H = N / 2, E = KK::LE, G = KK::LG, NG = KK::LNG;
+__global__ void __launch_bounds__(LK<N>::THREADS, LK<N>::MINB) k_c2r_z(SweepArgs a) {
+  using KK = LK<N>;
+  constexpr int H = N / 2, E = KK::E, G = KK::G, NG = KK::NG;
   constexpr long long NN = (long long)N * N;
   extern __shared__ float4 smem4[];
   float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* tws = tw + N;
   load_tw(tw, a.tw, N);
+  PlanRun<typename KK::P>::template fill<2>(tws, a.tw);
   __shared__ double red[kMaxBatch];
+  __shared__ float s_cb[kMaxBatch];
+  stage_params(s_cb, a.cb);
   if (threadIdx.x < kMaxBatch) red[threadIdx.x] = 0.0;
   __syncthreads();
   const int g = threadIdx.x / G, t = threadIdx.x % G;
-  float2* gbuf = tw + N + g * GroupBuf<H, 1>::size;
+  float2* gbuf = tws + KK::TW + g * KK::gsize;
   GroupSync<G> sync(g);
   const int lines = N * N;
   const bool want_sig = a.sig_acc != nullptr;
-  float sig[kMaxBatch];
-#pragma unroll
-  for (int b = 0; b < kMaxBatch; ++b) sig[b] = 0.f;
   for (int s = blockIdx.x; s * NG < lines; s += gridDim.x) {
     const int l = s * NG + g;
     const bool valid = l < lines;
     const int lv = valid ? l : 0;
-    const int ix = lv / N, iy = lv % N;
-    float zr[2 * E];
-    uint8_t am[2 * E];
+    const int ix = lv / N, iy = lv - (lv / N) * N;
+    float2 zr[E];
+    uint32_t am[E];  // the two argmax bytes of each element
     float* zline = a.zreion + (long long)lv * N;
     uint8_t* aline = a.argmax ? a.argmax + (long long)lv * N : nullptr;
     if (a.first || !valid) {
 #pragma unroll
-      for (int i = 0; i < 2 * E; ++i) { zr[i] = 0.f; am[i] = 255; }
+      for (int m = 0; m < E; ++m) {
+        zr[m] = make_float2(0.f, 0.f);
+        am[m] = 0xFFFFu;
+      }
     } else {
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int p = t + G * m;
-        float2 q = reinterpret_cast<const float2*>(zline)[p];
-        zr[2 * m] = q.x;
-        zr[2 * m + 1] = q.y;
-        if (aline) {
-          uchar2 u = reinterpret_cast<const uchar2*>(aline)[p];
-          am[2 * m] = u.x;
-          am[2 * m + 1] = u.y;
-        } else {
-          am[2 * m] = am[2 * m + 1] = 255;
-        }
+        zr[m] = reinterpret_cast<const float2*>(zline)[p];
+        am[m] = aline ? (uint32_t)reinterpret_cast<const uint16_t*>(aline)[p] : 0xFFFFu;
       }
     }
     for (int b = 0; b < a.nb; ++b) {
       const float2* slot = a.slots + (long long)b * a.slot_stride;
       const float2* src = slot + (long long)lv * H;
-      float2 v[1][E];
+      float2 v[E];
 #pragma unroll
-      for (int m = 0; m < E; ++m) v[0][m] = valid ? __ldg(src + t + G * m) : make_float2(0.f, 0.f);
+      for (int m = 0; m < E; ++m) v[m] = valid ? __ldg(src + t + G * m) : make_float2(0.f, 0.f);
       float2 xn = make_float2(0.f, 0.f);
       if (t == 0 && valid) xn = __ldg(slot + NN * H + (long long)iy * N + ix);
-      line_c2r<N>(v, xn, gbuf, t, tw, sync);
-      const float cb = a.cb[b];
-      const uint8_t rid = (uint8_t)(a.r0 + b);
+      line_c2r<N>(v, xn, gbuf, t, tw, tws, sync);
+      const float cb = s_cb[b];
+      const uint32_t rid = (uint32_t)(a.r0 + b);
       float ss = 0.f;
 #pragma unroll
       for (int m = 0; m < E; ++m) {
-        const float x0 = v[0][m].x, x1 = v[0][m].y;
+        const float x0 = v[m].x, x1 = v[m].y;
         const float z0 = fmaf(a.as, x0, cb), z1 = fmaf(a.as, x1, cb);
-        if (z0 > zr[2 * m]) { zr[2 * m] = z0; am[2 * m] = rid; }
-        if (z1 > zr[2 * m + 1]) { zr[2 * m + 1] = z1; am[2 * m + 1] = rid; }
+        if (z0 > zr[m].x) { zr[m].x = z0; am[m] = (am[m] & 0xFF00u) | rid; }
+        if (z1 > zr[m].y) { zr[m].y = z1; am[m] = (am[m] & 0x00FFu) | (rid << 8); }
         ss = fmaf(x0, x0, fmaf(x1, x1, ss));
       }
-      if (want_sig && valid) {
+      if (want_sig) {
+        if (!valid) ss = 0.f;
 #pragma unroll
-        for (int bb = 0; bb < kMaxBatch; ++bb)
-          if (bb == b) sig[bb] += ss;
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&red[b], (double)ss);
       }
     }
     if (valid) {
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int p = t + G * m;
-        reinterpret_cast<float2*>(zline)[p] = make_float2(zr[2 * m], zr[2 * m + 1]);
-        if (aline) reinterpret_cast<uchar2*>(aline)[p] = make_uchar2(am[2 * m], am[2 * m + 1]);
+        reinterpret_cast<float2*>(zline)[p] = zr[m];
+        if (aline) reinterpret_cast<uint16_t*>(aline)[p] = (uint16_t)am[m];
       }
     }
   }
   if (want_sig) {
-#pragma unroll
-    for (int b = 0; b < kMaxBatch; ++b) {
-      if (b < a.nb) {
-        float s = sig[b];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&red[b], (double)s);
-      }
-    }
     __syncthreads();
     if (threadIdx.x < a.nb) atomicAdd(&a.sig_acc[a.r0 + threadIdx.x], red[threadIdx.x]);
   }

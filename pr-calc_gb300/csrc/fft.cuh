@@ -1,9 +1,7 @@
 // fft.cuh — register/shared-memory Stockham FFT building blocks for sm_103a.
 //
 // One FFT of length L is carried by a *group* of G = L/E threads; thread t of
-// the group holds the E elements at positions t + G*m (m = 0..E-1) for C
-// independent columns (C = 2 lets one 16-byte access fetch two adjacent
-// pencils).  A mixed-radix Stockham autosort (Govindaraju et al., "High
+// the group holds the E elements at positions t + G*m (m = 0..E-1).  A mixed-radix Stockham autosort (Govindaraju et al., "High
 // performance discrete Fourier transforms on graphics processors", SC 2008)
 // runs stage by stage: with span Ns and radix R, virtual butterfly j reads
 // positions j + r*L/R and writes (j/Ns)*Ns*R + j%Ns + r*Ns.  Both the input
@@ -14,8 +12,8 @@
 // Sign convention: INV = true is FFTW's backward transform (e^{+2 pi i nk/L}),
 // INV = false the forward one (e^{-2 pi i nk/L}); neither is normalised.
 // Twiddles come from a table tw[i] = e^{+2 pi i i/NT} (NT = table length,
-// built in FP64 on the host, rounded to FP32); an L-point FFT reads it with
-// stride NT/L.
+// built in FP64 on the host, rounded to FP32), re-laid out per stage in shared
+// memory (TwFill) so that a warp's twiddle reads hit distinct banks.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -150,118 +148,144 @@ template <int... R> struct NumStages { static constexpr int v = sizeof...(R); };
 // groups of a warp always run the same stages, so a full-warp sync is safe).
 // G == 64: two warps, synchronised by a named barrier id 1 + group index.
 template <int G> struct GroupSync {
-  __device__ __forceinline__ explicit GroupSync(int /*group_in_cta*/) {}
-  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+  unsigned mask;
+  __device__ __forceinline__ explicit GroupSync(int /*group_in_cta*/, unsigned lanes = 0xffffffffu)
+      : mask(lanes) {}
+  __device__ __forceinline__ void operator()() const { __syncwarp(mask); }
 };
 template <> struct GroupSync<64> {
   int id;
-  __device__ __forceinline__ explicit GroupSync(int g) : id(1 + g) {}
+  __device__ __forceinline__ explicit GroupSync(int g, unsigned = 0xffffffffu) : id(1 + g) {}
   __device__ __forceinline__ void operator()() const {
     asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
   }
 };
 
 // ---------------------------------------------------------------- smem layout
-// Group buffer of L positions x C columns.  Positions are swizzled inside
-// blocks of 8 (C=2, 16-byte units) or 16 (C=1, 8-byte units) so that the
-// stride-R stores of the early stages do not pile onto one bank.
-template <int L, int C> struct Swz {
-  static constexpr int B = (C == 2) ? 8 : 16;
-  static constexpr bool on = (L % B) == 0;
-  static __device__ __forceinline__ int f(int p) { return on ? (p ^ ((p / B) & (B - 1))) : p; }
-};
-template <int L, int C> struct GroupBuf {
-  // float2 elements per group buffer, padded so neighbouring groups start on
-  // different banks
-  static constexpr int size = L * C + 4 * C;
+template <int L, int G = 32> struct GroupBuf {
+  // float2 elements per group buffer; groups narrower than one shared-memory
+  // wavefront (16 lanes x 8 B) are padded by one group access width so that
+  // the groups sharing a wavefront start on other banks
+  static constexpr int pad = G < 16 ? G : 0;
+  static constexpr int size = L + pad;
 };
 
-template <int L, int C>
-__device__ __forceinline__ void sm_put(float2* sm, int pos, const float2 (&a)[C]) {
-  int p = Swz<L, C>::f(pos);
-  if constexpr (C == 2) {
-    reinterpret_cast<float4*>(sm)[p] = make_float4(a[0].x, a[0].y, a[1].x, a[1].y);
-  } else {
-    sm[p] = a[0];
+// A group's exchange buffer of L positions (one column, 8-byte elements).
+// Positions are XOR-swizzled inside blocks of 16 (p ^ ((p >> 4) & 15)) when L
+// is a multiple of 16.  Because the swizzle is linear over GF(2), a position
+// tp | cp made of disjoint thread bits tp and compile-time bits cp maps to
+// X(tp) ^ X(cp): the thread part is computed once (thread()) and every access
+// costs one XOR with a constant.
+template <int L> struct LineBuf {
+  float2* sm;
+  static constexpr bool on = (L % 16) == 0;
+  static __device__ __forceinline__ constexpr int sw(int p) { return on ? (p ^ ((p >> 4) & 15)) : p; }
+  __device__ __forceinline__ int thread(int tp) const { return sw(tp); }
+  __device__ __forceinline__ float2 get(int h, int cp) const { return sm[h ^ sw(cp)]; }
+  __device__ __forceinline__ void put(int h, int cp, float2 v) const { sm[h ^ sw(cp)] = v; }
+  __device__ __forceinline__ float2 get_pos(int p) const { return sm[sw(p)]; }
+  __device__ __forceinline__ void put_pos(int p, float2 v) const { sm[sw(p)] = v; }
+};
+
+template <int X> struct IsPow2 { static constexpr bool v = X > 0 && (X & (X - 1)) == 0; };
+template <int... R> struct AllPow2;
+template <> struct AllPow2<> { static constexpr bool v = true; };
+template <int R0, int... R> struct AllPow2<R0, R...> {
+  static constexpr bool v = IsPow2<R0>::v && AllPow2<R...>::v;
+};
+
+// ---------------------------------------------------------------- twiddles
+// Per-stage twiddle tables.  The stage with span Ns > 1 and radix R reads
+// w^{r k}, w = e^{+2 pi i/(Ns R)}, for r = 1..R-1 and k = j mod Ns; it is stored
+// as tab[(r-1)*Ns + k] so that the lanes of a warp (consecutive k) read
+// consecutive words.  Stage tables follow each other in one array.
+template <int L, int Ns, int... Rs> struct TwSize;
+template <int L, int Ns> struct TwSize<L, Ns> { static constexpr int v = 0; };
+template <int L, int Ns, int R, int... Rest> struct TwSize<L, Ns, R, Rest...> {
+  static constexpr int v = (Ns > 1 ? (R - 1) * Ns : 0) + TwSize<L, Ns * R, Rest...>::v;
+};
+
+// Fills the stage tables from the N-entry table e^{+2 pi i k/NT}; TWS = NT/L.
+template <int L, int TWS, int Ns, int OFF, int... Rs> struct TwFill;
+template <int L, int TWS, int Ns, int OFF> struct TwFill<L, TWS, Ns, OFF> {
+  static __device__ __forceinline__ void run(float2*, const float2*) {}
+};
+template <int L, int TWS, int Ns, int OFF, int R, int... Rest> struct TwFill<L, TWS, Ns, OFF, R, Rest...> {
+  static __device__ __forceinline__ void run(float2* tab, const float2* tabN) {
+    if constexpr (Ns > 1) {
+      constexpr int STEP = (L / (Ns * R)) * TWS;
+      for (int i = threadIdx.x; i < (R - 1) * Ns; i += blockDim.x) {
+        const int r = i / Ns + 1, k = i - (i / Ns) * Ns;
+        tab[OFF + i] = tabN[r * k * STEP];
+      }
+    }
+    TwFill<L, TWS, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(tab, tabN);
   }
-}
-template <int L, int C>
-__device__ __forceinline__ void sm_get(const float2* sm, int pos, float2 (&a)[C]) {
-  int p = Swz<L, C>::f(pos);
-  if constexpr (C == 2) {
-    float4 q = reinterpret_cast<const float4*>(sm)[p];
-    a[0] = make_float2(q.x, q.y);
-    a[1] = make_float2(q.z, q.w);
-  } else {
-    a[0] = sm[p];
-  }
-}
+};
 
 // ---------------------------------------------------------------- Stockham
-// TWS = table stride (table length / L).
-template <int L, int E, int C, bool INV, int TWS, int Ns, int... Rs> struct Stages;
+// Buf provides thread(tp) / get(h, cp) / put(h, cp, v) for split positions and
+// get_pos / put_pos for general ones; SPLIT (power-of-two G and radices)
+// selects the former.  tws: the stage twiddle tables, OFF this stage's offset.
+template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF, int... Rs> struct Stages;
 
-template <int L, int E, int C, bool INV, int TWS, int Ns> struct Stages<L, E, C, INV, TWS, Ns> {
-  template <class Sync>
-  static __device__ __forceinline__ void run(float2 (&)[C][E], float2*, int, const float2*, const Sync&) {}
+template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF> struct Stages<L, E, INV, SPLIT, Ns, OFF> {
+  template <class Buf, class Sync>
+  static __device__ __forceinline__ void run(float2 (&)[E], const Buf&, int, const float2*, const Sync&) {}
 };
 
-template <int L, int E, int C, bool INV, int TWS, int Ns, int R, int... Rest>
-struct Stages<L, E, C, INV, TWS, Ns, R, Rest...> {
-  template <class Sync>
-  static __device__ __forceinline__ void run(float2 (&v)[C][E], float2* sm, int t,
-                                             const float2* tw, const Sync& sync) {
+template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF, int R, int... Rest>
+struct Stages<L, E, INV, SPLIT, Ns, OFF, R, Rest...> {
+  template <class Buf, class Sync>
+  static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, int t, const float2* tws,
+                                             const Sync& sync) {
     constexpr int G = L / E;
     constexpr int Q = E / R;
     static_assert(E % R == 0, "radix must divide the per-thread element count");
     constexpr bool last = (Ns * R == L);
-    constexpr int TSTEP = (L / (Ns * R)) * TWS;  // table step per unit of r*k
+    constexpr int NG = (Ns > G) ? Ns / G : 1;
+    // Store positions split into thread bits and constant bits: with Ns <= G,
+    // (t/Ns)*Ns*R + t%Ns  |  q*G*R + r*Ns; with Ns > G, t  |  (q/NG)*Ns*R +
+    // G*(q%NG) + r*Ns.
+    int hw = 0;
+    if constexpr (SPLIT && !last) hw = buf.thread(Ns <= G ? (t / Ns) * Ns * R + (t % Ns) : t);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int j = t + G * q;
       const int k = (Ns == 1) ? 0 : (j % Ns);
-      float2 a[C][R];
+      float2 a[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int c = 0; c < C; ++c) a[c][r] = v[c][q + r * Q];
+      for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
       if constexpr (Ns > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) {
-          const float2 w = twid<INV>(tw[r * k * TSTEP]);
-#pragma unroll
-          for (int c = 0; c < C; ++c) a[c][r] = cmul(a[c][r], w);
-        }
+        for (int r = 1; r < R; ++r) a[r] = cmul(a[r], twid<INV>(tws[OFF + (r - 1) * Ns + k]));
       }
-#pragma unroll
-      for (int c = 0; c < C; ++c) Dft<R, INV>::run(a[c]);
+      Dft<R, INV>::run(a);
       if constexpr (last) {
 #pragma unroll
-        for (int r = 0; r < R; ++r)
+        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+      } else if constexpr (SPLIT) {
 #pragma unroll
-          for (int c = 0; c < C; ++c) v[c][q + r * Q] = a[c][r];
+        for (int r = 0; r < R; ++r)
+          buf.put(hw, (Ns <= G) ? (q * G * R + r * Ns) : ((q / NG) * Ns * R + G * (q % NG) + r * Ns), a[r]);
       } else {
         const int base = (j / Ns) * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          float2 o[C];
-#pragma unroll
-          for (int c = 0; c < C; ++c) o[c] = a[c][r];
-          sm_put<L, C>(sm, base + r * Ns, o);
-        }
+        for (int r = 0; r < R; ++r) buf.put_pos(base + r * Ns, a[r]);
       }
     }
     if constexpr (!last) {
       sync();
+      if constexpr (SPLIT) {
+        const int hr = buf.thread(t);
 #pragma unroll
-      for (int m = 0; m < E; ++m) {
-        float2 o[C];
-        sm_get<L, C>(sm, t + G * m, o);
+        for (int m = 0; m < E; ++m) v[m] = buf.get(hr, G * m);
+      } else {
 #pragma unroll
-        for (int c = 0; c < C; ++c) v[c][m] = o[c];
+        for (int m = 0; m < E; ++m) v[m] = buf.get_pos(t + G * m);
       }
       sync();
-      Stages<L, E, C, INV, TWS, Ns * R, Rest...>::run(v, sm, t, tw, sync);
+      Stages<L, E, INV, SPLIT, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(v, buf, t, tws, sync);
     }
   }
 };
@@ -269,10 +293,18 @@ struct Stages<L, E, C, INV, TWS, Ns, R, Rest...> {
 template <class P> struct PlanRun;
 template <int E, int... R> struct PlanRun<Plan<E, R...>> {
   static constexpr int L = Prod<R...>::v;
-  template <int C, bool INV, int TWS, class Sync>
-  static __device__ __forceinline__ void run(float2 (&v)[C][E], float2* sm, int t,
-                                             const float2* tw, const Sync& sync) {
-    Stages<L, E, C, INV, TWS, 1, R...>::run(v, sm, t, tw, sync);
+  static constexpr int G = L / E;
+  static constexpr bool SPLIT = IsPow2<G>::v && AllPow2<R...>::v;
+  static constexpr int TW = TwSize<L, 1, R...>::v;  // stage-table entries
+  // stage tables from an NT-entry table (TWS = NT / L)
+  template <int TWS>
+  static __device__ __forceinline__ void fill(float2* tws, const float2* tabN) {
+    TwFill<L, TWS, 1, 0, R...>::run(tws, tabN);
+  }
+  template <bool INV, class Buf, class Sync>
+  static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, int t, const float2* tws,
+                                             const Sync& sync) {
+    Stages<L, E, INV, SPLIT, 1, 0, R...>::run(v, buf, t, tws, sync);
   }
 };
 
