@@ -168,6 +168,24 @@ int prc_d2z_profile_read(prc_d2z_ctx* ctx, double* ms /*PRC_NKINDS*/, long long*
 
 int prc_d2z_destroy(prc_d2z_ctx* ctx);
 
+/* prc_d2z_forward for small boxes without any device allocation.  No
+ * counterpart in the reference (pr-calc always allocates its FFTW buffers).
+ * For callers that must not allocate device memory when they ask for a
+ * result: a host framework that owns all device memory through its own pool,
+ * or a latency-critical stage that cannot afford cudaMalloc/cudaFree, which may
+ * synchronise the device.  The workspace is a fixed array inside the library
+ * (about 2.2 MB, held by every GPU that loads it) that fits grids up to N = 64
+ * (N in 8, 12, 16, 24, 32, 48, 64); larger N is rejected with PRC_ERR_INVALID.
+ * delta_lin, zreion and argmax (nullable) are device pointers, N^3 each, laid
+ * out as for prc_d2z_forward, whose zreion/argmax it reproduces; the call
+ * returns after the work on `stream` has finished.  The first call on a device
+ * performs a one-time set-up (it looks up the array's device address), so make
+ * it before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU race, so serialise them. */
+int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const double* radii_mpc,
+                           const double* barrier_b, double barrier_a, double growth_init,
+                           const float* delta_lin, float* zreion, uint8_t* argmax, void* stream);
+
 const char* prc_last_error(void);
 
 #ifdef __cplusplus

@@ -30,7 +30,7 @@ EXPORTS = [
     "prc_compute_tables", "prc_growth", "prc_sigma2", "prc_inverse_erfc", "prc_tau",
     "prc_d2z_supported", "prc_d2z_create", "prc_d2z_forward", "prc_d2z_smooth", "prc_d2z_history",
     "prc_d2z_backward", "prc_d2z_last_timing", "prc_d2z_last_launches", "prc_d2z_profile",
-    "prc_d2z_profile_read", "prc_d2z_destroy",
+    "prc_d2z_profile_read", "prc_d2z_destroy", "prc_d2z_forward_static",
     "prc_last_error",
 ]
 
@@ -98,6 +98,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_d2z_last_launches.argtypes = [vp, P(c_int)]
     L.prc_d2z_destroy.argtypes = [vp]
     L.prc_d2z_profile.argtypes = [vp, c_int]
+    L.prc_d2z_forward_static.argtypes = [c_int, c_int, c_double, vp, vp, c_double, c_double, vp, vp, vp, vp]
     L.prc_d2z_profile_read.argtypes = [vp, P(c_double), P(ctypes.c_longlong)]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or c_int
