@@ -135,6 +135,57 @@ int prc_d2z_smooth(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_device
 int prc_d2z_history(prc_d2z_ctx* ctx, const float* zreion, int zreion_on_device,
                     uint32_t* counts, float* history, float* history_z);
 
+/* ---- history correction (main_d2z.C:76-101) -------------------------------
+ * After the hot loop the reference turns the raw zreion field into its final
+ * form: GetBubbleMFP (bubble mean free path from random skewers), GetCHistory
+ * (the MFP-corrected ionisation history) and CorrectHistory (a per-cell map
+ * of zreion through that history).  These entry points restate them. */
+#define PRC_NCHISTORY 10000   /* allvars_d2z.h:5 */
+#define PRC_NX_MFP    1000    /* allvars_d2z.h:9 */
+#define PRC_NMFP      200     /* allvars_d2z.h:13 */
+#define PRC_NSKEWERS  20000   /* allvars_d2z.h:17 */
+
+/* Float2FloatTable (tables.C:9-38): f32 min, f32 max, i32 n, f32 table[n]. */
+typedef struct {
+  float minval, maxval, delta;
+  int n;
+  float* table;   /* malloc'd by prc_f2f_load, released by prc_f2f_free */
+} prc_f2f_table;
+int prc_f2f_load(const char* path, prc_f2f_table* t);
+float prc_f2f_eval(const prc_f2f_table* t, float x);
+void prc_f2f_free(prc_f2f_table* t);
+
+/* deltac and the Press-Schechter collapsed fraction (cosmology.C:141-172,311-324). */
+float prc_deltac(float z, float omegam, float omegal, float w, float* dcoll);
+float prc_fcoll(float z, float zInit, float omegam, float omegal, float w, float sigma_min);
+
+/* GetBubbleMFP (bubblehistory_d2z.C:82-252) at one rank: for n_x ionised
+ * fractions x (0.01..0.999) and n_skewers random ionised start cells each
+ * (glibc rand() from its unseeded state, as the reference draws them), walk
+ * along y and z to the first neutral cell.  Outputs mfp[n_x], mfp_x[n_x] and
+ * dfdmfp[PRC_NMFP * n_x].  zreion is a host grid (the rejection sampling of
+ * the starts reads it); the walks run on the device. */
+typedef struct {
+  int N;
+  float box_mpc;      /* BoxSize / h */
+  int n_x;            /* PRC_NX_MFP in the reference */
+  int n_skewers;      /* PRC_NSKEWERS in the reference */
+} prc_mfp_setup;
+int prc_d2z_bubble_mfp(prc_d2z_ctx* ctx, const prc_mfp_setup* s, const float* zreion_host,
+                       const float* history, float* mfp, float* mfp_x, float* dfdmfp);
+
+/* GetCHistory (bubblehistory_d2z.C:45-80): chistory[PRC_NCHISTORY] from the
+ * fcoll table, the MFP curve (n_x points), rmfp (the -r value) and zeta. */
+int prc_chistory(const prc_f2f_table* fcoll, const float* mfp, int n_x, float rmfp, float zeta,
+                 float* chistory);
+/* CorrectHistory's map (bubblehistory_d2z.C:314-326): zvz[PRC_NHISTORY]. */
+int prc_zvz(const float* history, const float* chistory, float* zvz);
+/* CorrectHistory's per-cell step (bubblehistory_d2z.C:328-341) on the device:
+ * zreion = zvz[(int)((zreion - 49.9)/dz)].  Cells whose bin falls outside the
+ * table (z > 50.4 or z < 0.01; the reference reads out of bounds there) are
+ * left unchanged. */
+int prc_d2z_correct(prc_d2z_ctx* ctx, const float* zvz, float* zreion, int zreion_on_device);
+
 /* Adjoint of prc_d2z_forward (no reference counterpart: the reference has no
  * gradient).  dL_dz (N^3) and argmax (N^3) -> dL/d delta_lin (N^3) and
  * dL/dB_r (n_radii doubles, optional).  The host maps dL/dB_r to dL/dzeta and

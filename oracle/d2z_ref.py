@@ -415,7 +415,8 @@ def history(zreion: np.ndarray):
     hist = (counts.astype(f32).astype(f64) / n3).astype(f32)
     for i in range(1, NHISTORY):
         hist[i] = f32(hist[i] + hist[i - 1])
-    hz = np.array([f32(HISTORY_INITIAL + i * f64(dzf)) for i in range(NHISTORY)], f32)
+    # i*dz is an int x float product, rounded to float before the double sum
+    hz = np.array([f32(HISTORY_INITIAL + f64(f32(i * dzf))) for i in range(NHISTORY)], f32)
     return counts, hist, hz
 
 

@@ -19,6 +19,7 @@
 #include "d2z_adjoint.cuh"
 #include "d2z_dispatch.h"
 #include "errors.h"
+#include "history.h"
 
 namespace prc {
 #define PRC_DECL(NV) const KernelSet* kernel_set_##NV();
@@ -72,6 +73,52 @@ __global__ void k_hist(const float* __restrict__ z, long long n, uint32_t* count
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     const int leader = __ffs(peers) - 1;
     if (ok && (int)(threadIdx.x & 31) == leader) atomicAdd(&counts[bin], (uint32_t)__popc(peers));
+  }
+}
+
+// ------------------------------------------------------------ skewer walks
+// GetBubbleMFP's walks (bubblehistory_d2z.C:159-183 and :197-221): from each
+// start cell step along +y (then +z), periodically, until the first cell with
+// zreion < zcur or back at the start; steps = number of moves.  At most N
+// moves per walk.
+__global__ void k_walks(const float* __restrict__ z, int N, const int* __restrict__ start,
+                        const float* __restrict__ zcur, int ns, long long total, int* steps) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < total; s += stride) {
+    const float zc = zcur[s / ns];
+    const int i = start[3 * s], j0 = start[3 * s + 1], k0 = start[3 * s + 2];
+    const float* plane = z + (long long)i * N * N;
+    int j = j0, m = 0;
+    for (;;) {
+      if (++j >= N) j -= N;
+      ++m;
+      if (plane[(long long)j * N + k0] < zc || j == j0) break;
+    }
+    steps[2 * s] = m;
+    const float* line = plane + (long long)j0 * N;
+    int k = k0;
+    m = 0;
+    for (;;) {
+      if (++k >= N) k -= N;
+      ++m;
+      if (line[k] < zc || k == k0) break;
+    }
+    steps[2 * s + 1] = m;
+  }
+}
+
+// CorrectHistory's per-cell map (bubblehistory_d2z.C:328-341) with the bin of
+// k_hist; bins outside the table leave the cell unchanged.
+__global__ void k_remap(float* __restrict__ z, long long n, const float* __restrict__ zvz, double dzd) {
+  const float inv = (float)(1.0 / dzd);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float zc = z[i];
+    const float qf = (zc - 49.9f) * inv;
+    if (!(fabsf(qf) < 1e9f)) continue;
+    const float r = rintf(qf);
+    const int bin = (fabsf(qf - r) < 0.05f) ? (int)(((double)zc - 49.9) / dzd) : (int)qf;
+    if (bin >= 0 && bin < kNHistory) z[i] = __ldg(zvz + bin);
   }
 }
 
@@ -520,7 +567,8 @@ int prc_d2z_history(prc_d2z_ctx* c, const float* zreion, int zreion_on_device, u
   for (int i = 1; i < kNHistory; ++i) history[i] += history[i - 1];
   if (history_z) {
     history_z[0] = (float)49.9;
-    for (int i = 1; i < kNHistory; ++i) history_z[i] = (float)(49.9 + i * (double)dzf);
+    // i*dz is an int x float product (float), then the double sum (bubblehistory_d2z.C:34)
+    for (int i = 1; i < kNHistory; ++i) history_z[i] = (float)(49.9 + (double)(i * dzf));
   }
   return PRC_OK;
 }
@@ -606,6 +654,77 @@ int prc_d2z_backward(prc_d2z_ctx* c, const float* dL_dz, const uint8_t* argmax, 
   c->last_ms[1] = t0;
   c->last_ms[2] = t0 + t1;
   c->have_timing = 1;
+  return PRC_OK;
+}
+
+int prc_d2z_bubble_mfp(prc_d2z_ctx* c, const prc_mfp_setup* s, const float* zreion_host, const float* history,
+                       float* mfp, float* mfp_x, float* dfdmfp) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!s || !zreion_host || !history || !mfp || !mfp_x || !dfdmfp)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_bubble_mfp: null argument");
+  if (s->N != c->N) return prc_fail(PRC_ERR_INVALID, "prc_d2z_bubble_mfp: N=%d but the context has N=%d", s->N, c->N);
+  if ((st = set_device(c)) != PRC_OK) return st;
+  prc_hist::MfpPlan plan;
+  if ((st = prc_hist::mfp_plan(s, zreion_host, history, &plan)) != PRC_OK) return st;
+  const long long n3 = c->NN * c->N;
+  const long long total = (long long)plan.nx * plan.ns;
+  if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "zreion")) != PRC_OK) return st;
+  int *d_start = nullptr, *d_steps = nullptr;
+  float* d_zcur = nullptr;
+  if ((st = dalloc(&d_start, (size_t)total * 3, "skewer starts")) != PRC_OK) return st;
+  if ((st = dalloc(&d_steps, (size_t)total * 2, "skewer steps")) != PRC_OK) {
+    cudaFree(d_start);
+    return st;
+  }
+  if ((st = dalloc(&d_zcur, (size_t)plan.nx, "skewer redshifts")) != PRC_OK) {
+    cudaFree(d_start);
+    cudaFree(d_steps);
+    return st;
+  }
+  std::vector<int> steps((size_t)total * 2);
+  cudaError_t e = cudaMemcpyAsync(c->zre, zreion_host, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_start, plan.start.data(), sizeof(int) * 3 * total, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_zcur, plan.zcur.data(), sizeof(float) * plan.nx, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) {
+    k_walks<<<c->sms * 16, 256, 0, c->st>>>(c->zre, c->N, d_start, d_zcur, plan.ns, total, d_steps);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(steps.data(), d_steps, sizeof(int) * 2 * total, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(d_start);
+  cudaFree(d_steps);
+  cudaFree(d_zcur);
+  if (e != cudaSuccess) return cuda_fail(e, "prc_d2z_bubble_mfp");
+  prc_hist::mfp_finish(plan, steps.data(), mfp, mfp_x, dfdmfp);
+  return PRC_OK;
+}
+
+int prc_d2z_correct(prc_d2z_ctx* c, const float* zvz, float* zreion, int on_device) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!zvz || !zreion) return prc_fail(PRC_ERR_INVALID, "prc_d2z_correct: null argument");
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const long long n3 = c->NN * c->N;
+  float* d_z = zreion;
+  if (!on_device) {
+    if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "zreion")) != PRC_OK) return st;
+    PRC_CU(cudaMemcpyAsync(c->zre, zreion, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D zreion");
+    d_z = c->zre;
+  }
+  float* d_zvz = nullptr;
+  if ((st = dalloc(&d_zvz, (size_t)kNHistory, "zvz")) != PRC_OK) return st;
+  const float dzf = (float)((0.01 - 49.9) / (100000 - 1));
+  cudaError_t e = cudaMemcpyAsync(d_zvz, zvz, sizeof(float) * kNHistory, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) {
+    k_remap<<<c->sms * 8, 256, 0, c->st>>>(d_z, n3, d_zvz, (double)dzf);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && !on_device)
+    e = cudaMemcpyAsync(zreion, d_z, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(d_zvz);
+  if (e != cudaSuccess) return cuda_fail(e, "prc_d2z_correct");
   return PRC_OK;
 }
 

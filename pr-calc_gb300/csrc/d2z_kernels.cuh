@@ -87,7 +87,7 @@ template <int N> struct TK {
   static_assert(H % T == 0 && N % T == 0 && T % 2 == 0, "tile width");
   static constexpr int THREADS = T * G;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
-  static constexpr int smem_f2 = TW + N * T;
+  static constexpr int smem_f2 = TW + 2 * N * T;       // twiddles + two tiles
   // resident CTAs per SM the register budget is sized for; the accumulate
   // mode keeps E more complex values per thread
   static constexpr int MINB = THREADS >= 512 ? 2 : (THREADS >= 256 ? 3 : 4);
@@ -228,47 +228,91 @@ template <int N> struct TileCol {
   __device__ __forceinline__ void put_pos(int p, float2 v) const { tile[S::idx(p, col)] = v; }
 };
 
-// Cooperative tile traffic: 16-byte chunks (two columns), consecutive threads
-// along a row, a warp covering whole row segments.  Thread rows are tp =
-// tid / CPR, iteration i adds the constant row i * RPI.
-template <int N, int THREADS> struct TileIO {
+// Asynchronous 8-byte global -> shared copies (cp.async), so that the next
+// tile streams in while the current one is transformed.
+__device__ __forceinline__ void cp_async8(float2* smem, const float2* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int K> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
+}
+
+// Cooperative tile traffic, one 8-byte word per thread per row step: thread
+// (tp, c) = (tid / T, tid % T) moves column c of rows tp + G*i (i < E), so a
+// warp covers whole row segments; it is the transpose of the FFT mapping
+// (group = column, lane t = rows t + G*m).
+template <int N> struct TileIO {
+  static constexpr int T = TCfg<N>::T, G = TK<N>::G, E = TK<N>::E;
+  const int tp, c;
+  int h;
+  __device__ __forceinline__ TileIO(float2* tile) : tp(threadIdx.x / T), c(threadIdx.x % T) {
+    h = TileCol<N>{tile, c}.thread(tp);
+  }
+  __device__ __forceinline__ void load_async(float2* tile, const float2* base, int row_stride) const {
+    const float2* src = base + (long long)tp * row_stride + c;
+    const long long step = (long long)G * row_stride;
+#pragma unroll
+    for (int i = 0; i < E; ++i) cp_async8(tile + TileCol<N>::off(h, i * G), src + i * step);
+  }
+  __device__ __forceinline__ void store(const float2* tile, float2* base, int row_stride) const {
+    float2* dst = base + (long long)tp * row_stride + c;
+    const long long step = (long long)G * row_stride;
+#pragma unroll
+    for (int i = 0; i < E; ++i) dst[i * step] = tile[TileCol<N>::off(h, i * G)];
+  }
+  // base += tile (base = 0 first if zero)
+  __device__ __forceinline__ void accumulate(const float2* tile, float2* base, int row_stride, bool zero) const {
+    float2* dst = base + (long long)tp * row_stride + c;
+    const long long step = (long long)G * row_stride;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const float2 a = tile[TileCol<N>::off(h, i * G)];
+      float2 o = zero ? make_float2(0.f, 0.f) : dst[i * step];
+      dst[i * step] = make_float2(o.x + a.x, o.y + a.y);
+    }
+  }
+};
+
+// Synchronous cooperative tile traffic in 16-byte chunks (two columns):
+// consecutive threads along a row, thread rows tp = tid / CPR, iteration i
+// adding the constant row i * RPI.  Fewer, wider instructions than TileIO;
+// used by the passes that do not prefetch.
+template <int N, int THREADS> struct TileIO16 {
   static constexpr int T = TCfg<N>::T, CPR = T / 2, RPI = THREADS / CPR, ITER = N / RPI;
   static_assert(THREADS % CPR == 0 && N % RPI == 0, "tile io shape");
   const int tp, cc;
-  TileCol<N> c0, c1;
   int h0, h1;
-  __device__ __forceinline__ TileIO(float2* tile)
-      : tp(threadIdx.x / CPR), cc(threadIdx.x % CPR), c0{tile, 2 * (threadIdx.x % CPR)},
-        c1{tile, 2 * (threadIdx.x % CPR) + 1} {
-    h0 = c0.thread(tp);
-    h1 = c1.thread(tp);
+  __device__ __forceinline__ TileIO16() : tp(threadIdx.x / CPR), cc(threadIdx.x % CPR) {
+    h0 = TileCol<N>{nullptr, 2 * cc}.thread(tp);
+    h1 = TileCol<N>{nullptr, 2 * cc + 1}.thread(tp);
   }
-  __device__ __forceinline__ void load(const float2* base, int row_stride) const {
+  __device__ __forceinline__ void load(float2* tile, const float2* base, int row_stride) const {
     const float2* src = base + (long long)tp * row_stride + 2 * cc;
     const long long step = (long long)RPI * row_stride;
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
       const float4 v = __ldg(reinterpret_cast<const float4*>(src + i * step));
-      c0.put(h0, i * RPI, make_float2(v.x, v.y));
-      c1.put(h1, i * RPI, make_float2(v.z, v.w));
+      tile[TileCol<N>::off(h0, i * RPI)] = make_float2(v.x, v.y);
+      tile[TileCol<N>::off(h1, i * RPI)] = make_float2(v.z, v.w);
     }
   }
-  __device__ __forceinline__ void store(float2* base, int row_stride) const {
+  __device__ __forceinline__ void store(const float2* tile, float2* base, int row_stride) const {
     float2* dst = base + (long long)tp * row_stride + 2 * cc;
     const long long step = (long long)RPI * row_stride;
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
-      const float2 a = c0.get(h0, i * RPI), b = c1.get(h1, i * RPI);
+      const float2 a = tile[TileCol<N>::off(h0, i * RPI)], b = tile[TileCol<N>::off(h1, i * RPI)];
       *reinterpret_cast<float4*>(dst + i * step) = make_float4(a.x, a.y, b.x, b.y);
     }
   }
-  // base += tile (base = 0 first if zero)
-  __device__ __forceinline__ void accumulate(float2* base, int row_stride, bool zero) const {
+  __device__ __forceinline__ void accumulate(const float2* tile, float2* base, int row_stride, bool zero) const {
     float2* dst = base + (long long)tp * row_stride + 2 * cc;
     const long long step = (long long)RPI * row_stride;
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
-      const float2 a = c0.get(h0, i * RPI), b = c1.get(h1, i * RPI);
+      const float2 a = tile[TileCol<N>::off(h0, i * RPI)], b = tile[TileCol<N>::off(h1, i * RPI)];
       float4* d = reinterpret_cast<float4*>(dst + i * step);
       float4 o = zero ? make_float4(0.f, 0.f, 0.f, 0.f) : *d;
       o.x += a.x;
@@ -294,8 +338,12 @@ __device__ __forceinline__ void tile_store_t(const float2* tile, float2* out, in
 // ============================================================ column pass
 // One kernel for every column pass:
 //   TM_FWD / TM_INV  plain forward / inverse transform, in -> out (blockIdx.y
-//                    selects a slot), same layout or transposed;
-//   TM_WIN           per radius b: spectrum * W_b (k = 0 -> 0), inverse, -> slot b;
+//                    selects a slot), same layout or transposed; two tile
+//                    buffers, the next tile prefetched with cp.async;
+//   TM_WIN           spectrum tile loaded once (raw buffer, next one
+//                    prefetched during the last radius), then per radius b:
+//                    raw * W_b (k = 0 -> 0), inverse transform in the work
+//                    buffer, -> slot b;
 //   TM_ACC           per radius b: forward transform of slot b, acc += W_b * (.).
 // Rows ix and N-ix share |k|, so in the window modes each pair of rows is
 // evaluated once and handed to the mirror lane by a shuffle.
@@ -306,100 +354,181 @@ __global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_A
   constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, TH = KK::THREADS;
   constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);
   constexpr bool WIN = (MODE == TM_WIN || MODE == TM_ACC);
+  constexpr bool SPLIT = PlanRun<typename KK::P>::SPLIT;
   extern __shared__ float4 smem4[];
   float2* tws = reinterpret_cast<float2*>(smem4);  // stage twiddles
-  float2* tile = tws + KK::TW;
+  float2* buf0 = tws + KK::TW;
+  float2* buf1 = buf0 + N * T;
   __shared__ float s_kr[kMaxBatch];
   if constexpr (WIN) stage_params(s_kr, a.kr);
   PlanRun<typename KK::P>::template fill<1>(tws, a.tw);
-  __syncthreads();
   const int g = threadIdx.x / G, t = threadIdx.x - (threadIdx.x / G) * G;
   // CTAs smaller than a warp (the smallest grids) name only their own lanes
   constexpr unsigned LANES = TH >= 32 ? 0xffffffffu : ((1u << TH) - 1u);
   GroupSync<G> sync(g, LANES);
-  const TileCol<N> col{tile, g};
-  const TileIO<N, TH> io(tile);
-  constexpr bool SPLIT = PlanRun<typename KK::P>::SPLIT;
-  const int hrow = col.thread(t);  // rows t + G*m of this group's column
+  const TileIO<N> io(buf0);
+  const int hrow = TileCol<N>{buf0, g}.thread(t);  // rows t + G*m of this group's column (same in both buffers)
   const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
   const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;
   const int tiles = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;
-  for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+
+  struct Where {
+    TileSeg sg;
+    int outer, tc;
+    long long off;
+  };
+  auto where = [&](int ti) {
+    Where w;
     const bool sn = ti >= tiles0;
-    const TileSeg sg = sn ? a.seg[1] : a.seg[0];
+    w.sg = sn ? a.seg[1] : a.seg[0];
     const int tl = sn ? ti - tiles0 : ti;
-    const int outer = tl / sg.tpo, tc = tl - (tl / sg.tpo) * sg.tpo;
-    const long long off = (long long)outer * sg.outer_stride + (long long)tc * T;
-    // squared frequency of this group's column, without the row part
-    int syz = 0;
-    if constexpr (WIN) {
-      const int c = tc * T + g;
-      syz = sg.nyq ? fsq(c, N) + H * H : fsq(outer, N) + c * c;
-    }
-    const int nrad = WIN ? a.nb : 1;
-    float2 acc[E];
-    if constexpr (MODE == TM_ACC) {
+    w.outer = tl / w.sg.tpo;
+    w.tc = tl - w.outer * w.sg.tpo;
+    w.off = (long long)w.outer * w.sg.outer_stride + (long long)w.tc * T;
+    return w;
+  };
+  auto col_read = [&](const float2* tile, float2 (&v)[E]) {
+    const TileCol<N> col{const_cast<float2*>(tile), g};
 #pragma unroll
-      for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
+    for (int m = 0; m < E; ++m) v[m] = SPLIT ? col.get(hrow, G * m) : col.get_pos(t + G * m);
+  };
+  auto col_write = [&](float2* tile, const float2 (&v)[E]) {
+    const TileCol<N> col{tile, g};
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      if constexpr (SPLIT) col.put(hrow, G * m, v[m]);
+      else col.put_pos(t + G * m, v[m]);
     }
-    for (int b = 0; b < nrad; ++b) {
-      const float2* src = sg.in + off + yoff + (MODE == TM_ACC ? (long long)b * a.slot_stride : 0);
-      io.load(src, sg.row_stride);
+  };
+  auto window = [&](const Where& w, int b, float (&wv)[E]) {
+    const float kr = s_kr[b];
+    const int c = w.tc * T + g;
+    const int syz = w.sg.nyq ? fsq(c, N) + H * H : fsq(w.outer, N) + c * c;
+    constexpr int EH = E / 2;
+    constexpr bool share = (G <= 32);
+#pragma unroll
+    for (int m = 0; m < E; ++m)
+      if (!share || m <= EH) wv[m] = window_of(fsq(t + G * m, N) + syz, kr);
+    if constexpr (share) {
+#pragma unroll
+      for (int m = EH + 1; m < E; ++m) {
+        const float o = __shfl_sync(LANES, wv[E - 1 - m], (G - t) & (G - 1), G);
+        wv[m] = (t == 0) ? wv[E - m] : o;
+      }
+    }
+  };
+  // v *= W_b in place; only the E/2+1 directly evaluated values stay live
+  auto apply_window = [&](int ti, int b, float2 (&v)[E]) {
+    const Where w = where(ti);
+    const float kr = s_kr[b];
+    const int c = w.tc * T + g;
+    const int syz = w.sg.nyq ? fsq(c, N) + H * H : fsq(w.outer, N) + c * c;
+    constexpr int EH = E / 2;
+    if constexpr (G <= 32) {
+      float wv[EH + 1];
+#pragma unroll
+      for (int m = 0; m <= EH; ++m) {
+        wv[m] = window_of(fsq(t + G * m, N) + syz, kr);
+        v[m] = cscale(v[m], wv[m]);
+      }
+#pragma unroll
+      for (int m = EH + 1; m < E; ++m) {
+        const float o = __shfl_sync(LANES, wv[E - 1 - m], (G - t) & (G - 1), G);
+        v[m] = cscale(v[m], (t == 0) ? wv[E - m] : o);
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = cscale(v[m], window_of(fsq(t + G * m, N) + syz, kr));
+    }
+  };
+  auto store_tile = [&](const Where& w, const float2* tile, float2* dst) {
+    if (w.sg.transpose)
+      tile_store_t<N, T, TH>(tile, dst + (long long)w.outer * w.sg.outer_stride, w.tc * T);
+    else
+      io.store(tile, dst + w.off, w.sg.row_stride);
+  };
+
+  if constexpr (MODE == TM_FWD || MODE == TM_INV) {
+    const TileIO16<N, TH> io16;
+    for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      io16.load(buf0, w.sg.in + w.off + yoff, w.sg.row_stride);
       __syncthreads();
       float2 v[E];
-#pragma unroll
-      for (int m = 0; m < E; ++m) v[m] = SPLIT ? col.get(hrow, G * m) : col.get_pos(t + G * m);
-      float w[E];
-      if constexpr (WIN) {
-        const float kr = s_kr[b];
-        constexpr int EH = E / 2;
-        constexpr bool share = (G <= 32);
-#pragma unroll
-        for (int m = 0; m < E; ++m)
-          if (!share || m <= EH) w[m] = window_of(fsq(t + G * m, N) + syz, kr);
-        if constexpr (share) {
-#pragma unroll
-          for (int m = EH + 1; m < E; ++m) {
-            const float o = __shfl_sync(LANES, w[E - 1 - m], (G - t) & (G - 1), G);
-            w[m] = (t == 0) ? w[E - m] : o;
-          }
-        }
-      }
-      if constexpr (MODE == TM_WIN) {
-#pragma unroll
-        for (int m = 0; m < E; ++m) v[m] = cscale(v[m], w[m]);
-      }
+      col_read(buf0, v);
+      const TileCol<N> col{buf0, g};
       PlanRun<typename KK::P>::template run<INV>(v, col, t, tws, sync);
-      if constexpr (MODE == TM_ACC) {
-#pragma unroll
-        for (int m = 0; m < E; ++m) {
-          acc[m].x = fmaf(w[m], v[m].x, acc[m].x);
-          acc[m].y = fmaf(w[m], v[m].y, acc[m].y);
+      col_write(buf0, v);
+      __syncthreads();
+      if (w.sg.transpose)
+        tile_store_t<N, T, TH>(buf0, w.sg.out + yoff + (long long)w.outer * w.sg.outer_stride, w.tc * T);
+      else
+        io16.store(buf0, w.sg.out + yoff + w.off, w.sg.row_stride);
+      __syncthreads();
+    }
+  } else if constexpr (MODE == TM_WIN) {
+    float2* raw = buf0;
+    float2* work = buf1;
+    int ti = blockIdx.x;
+    if (ti < tiles) {
+      const Where w0 = where(ti);
+      io.load_async(raw, w0.sg.in + w0.off, w0.sg.row_stride);
+    }
+    cp_async_commit();
+    for (; ti < tiles; ti += gridDim.x) {
+      cp_async_wait<0>();
+      __syncthreads();
+      for (int b = 0; b < a.nb; ++b) {
+        float2 v[E];
+        col_read(raw, v);
+        if (b == a.nb - 1) {
+          // every group has its raw column: stream the next spectrum tile in
+          __syncthreads();
+          const int tn = ti + gridDim.x;
+          if (tn < tiles) {
+            const Where wn = where(tn);
+            io.load_async(raw, wn.sg.in + wn.off, wn.sg.row_stride);
+          }
+          cp_async_commit();
         }
-        __syncthreads();  // the next radius reloads the tile
-      } else {
-#pragma unroll
-        for (int m = 0; m < E; ++m) {
-          if constexpr (SPLIT) col.put(hrow, G * m, v[m]);
-          else col.put_pos(t + G * m, v[m]);
-        }
+        apply_window(ti, b, v);
+        const TileCol<N> col{work, g};
+        PlanRun<typename KK::P>::template run<true>(v, col, t, tws, sync);
+        col_write(work, v);
         __syncthreads();
-        float2* dst = sg.out + yoff + (MODE == TM_WIN ? (long long)b * a.slot_stride : 0);
-        if (sg.transpose)
-          tile_store_t<N, T, TH>(tile, dst + (long long)outer * sg.outer_stride, tc * T);
-        else
-          io.store(dst + off, sg.row_stride);
+        const Where w = where(ti);
+        store_tile(w, work, w.sg.out + (long long)b * a.slot_stride);
         __syncthreads();
       }
     }
-    if constexpr (MODE == TM_ACC) {
+    cp_async_wait<0>();
+  } else {  // TM_ACC
+    const TileIO16<N, TH> io16;
+    float2* tile = buf0;
+    for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      float2 acc[E];
 #pragma unroll
-      for (int m = 0; m < E; ++m) {
-        if constexpr (SPLIT) col.put(hrow, G * m, acc[m]);
-        else col.put_pos(t + G * m, acc[m]);
+      for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
+      for (int b = 0; b < a.nb; ++b) {
+        io16.load(tile, w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride);
+        __syncthreads();
+        float2 v[E];
+        col_read(tile, v);
+        float wv[E];
+        window(w, b, wv);
+        const TileCol<N> col{tile, g};
+        PlanRun<typename KK::P>::template run<false>(v, col, t, tws, sync);
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          acc[m].x = fmaf(wv[m], v[m].x, acc[m].x);
+          acc[m].y = fmaf(wv[m], v[m].y, acc[m].y);
+        }
+        __syncthreads();  // the next radius reloads the tile
       }
+      col_write(tile, acc);
       __syncthreads();
-      io.accumulate(sg.out + off, sg.row_stride, a.first != 0);
+      io16.accumulate(tile, w.sg.out + w.off, w.sg.row_stride, a.first != 0);
       __syncthreads();
     }
   }

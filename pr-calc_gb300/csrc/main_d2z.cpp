@@ -284,12 +284,60 @@ int main(int argc, char* argv[]) {
   if (prc_d2z_last_timing(ctx, ms) == PRC_OK)
     printf("\n GPU time: forward R2C %.3f ms, %d radii %.3f ms", ms[0], P.Nscales, ms[1]);
 
-  // GetHistory (bubblehistory_d2z.C:5-43) and tau (main_d2z.C:97-98)
+  // GetHistory (main_d2z.C:76, bubblehistory_d2z.C:5-43)
   std::vector<float> hist(PRC_NHISTORY), histz(PRC_NHISTORY);
   if ((st = prc_d2z_history(ctx, zreion.data(), 0, nullptr, hist.data(), histz.data())) != PRC_OK)
     return fail("prc_d2z_history", st);
 
-  // WriteZreionFile (io_d2z.C:209-245)
+  // GetBubbleMFP (main_d2z.C:79) with WriteMFP / WriteMFPPDF (io_d2z.C:343-402)
+  prc_mfp_setup mset;
+  mset.N = N;
+  mset.box_mpc = P.BoxSize / P.h;
+  mset.n_x = PRC_NX_MFP;
+  mset.n_skewers = PRC_NSKEWERS;
+  std::vector<float> mfp(PRC_NX_MFP), mfp_x(PRC_NX_MFP), dfdmfp((size_t)PRC_NMFP * PRC_NX_MFP);
+  if ((st = prc_d2z_bubble_mfp(ctx, &mset, zreion.data(), hist.data(), mfp.data(), mfp_x.data(), dfdmfp.data())) !=
+      PRC_OK)
+    return fail("prc_d2z_bubble_mfp", st);
+  printf("\n Writing bubble mfp...");
+  {
+    std::string f = std::string(CL.Basename) + ".mfp";
+    FILE* fd = fopen(f.c_str(), "w");
+    if (!fd) {
+      printf("\n File %s could not be opened\n\n", f.c_str());
+      return 1;
+    }
+    for (int i = 0; i < PRC_NX_MFP; i++) fprintf(fd, "%f %f\n", mfp_x[i], mfp[i]);
+    fclose(fd);
+  }
+  printf("\n Writing bubble mfp...");
+  {
+    std::string f = std::string(CL.Basename) + ".mfppdf";
+    FILE* fd = fopen(f.c_str(), "wb");
+    if (!fd) {
+      printf("\n File %s could not be opened\n\n", f.c_str());
+      return 1;
+    }
+    const float box = P.BoxSize / P.h, cell = box / N;
+    const int h1[2] = {PRC_NX_MFP, PRC_NMFP};
+    const float h2[4] = {0.01f, 0.999f, (float)log10(1 * cell), (float)log10(1.0 * box)};
+    fwrite(h1, sizeof(int), 2, fd);
+    fwrite(h2, sizeof(float), 4, fd);
+    fwrite(dfdmfp.data(), sizeof(float), dfdmfp.size(), fd);
+    fclose(fd);
+  }
+
+  // GetCHistory (main_d2z.C:84) and CorrectHistory (:87); both need the
+  // collapsed-fraction table fcoll_table.tab in the working directory
+  prc_f2f_table fct;
+  if ((st = prc_f2f_load("fcoll_table.tab", &fct)) != PRC_OK) return fail("reading fcoll_table.tab", st);
+  std::vector<float> chist(PRC_NCHISTORY), zvz(PRC_NHISTORY);
+  if ((st = prc_chistory(&fct, mfp.data(), PRC_NX_MFP, CL.Rmax, CL.zeta, chist.data())) != PRC_OK)
+    return fail("prc_chistory", st);
+  if ((st = prc_zvz(hist.data(), chist.data(), zvz.data())) != PRC_OK) return fail("prc_zvz", st);
+  if ((st = prc_d2z_correct(ctx, zvz.data(), zreion.data(), 0)) != PRC_OK) return fail("prc_d2z_correct", st);
+
+  // WriteZreionFile (main_d2z.C:90, io_d2z.C:209-245)
   printf("\n Writing reionization redshifts...");
   std::string zname = std::string(CL.Basename) + ".zreion";
   if (!write_all(zname.c_str(), zreion.data(), sizeof(float) * n3)) {
@@ -298,16 +346,19 @@ int main(int argc, char* argv[]) {
   }
   printf("\n Reionization redshifts written...");
   if (P.RecordBubbleSizes == 1) {
-    // WriteRbubbleFile (io_d2z.C:248-282): R of the winning scale, 0 where none won
+    // the .rbubble writer (io_d2z.C:248-282; its call is commented out at
+    // main_d2z.C:95): R of the winning scale, 0 where none won
     std::vector<float> rb((size_t)n3);
     for (long long i = 0; i < n3; ++i) rb[i] = argmax[i] == PRC_ARGMAX_NONE ? 0.f : (float)R[argmax[i]];
     std::string rname = std::string(CL.Basename) + ".rbubble";
     write_all(rname.c_str(), rb.data(), sizeof(float) * n3);
     printf("\n Bubble sizes written...");
   }
+  // GetHistory of the corrected field, tau (main_d2z.C:97-98), WriteHistory (:101)
+  if ((st = prc_d2z_history(ctx, zreion.data(), 0, nullptr, hist.data(), histz.data())) != PRC_OK)
+    return fail("prc_d2z_history", st);
   const float tau = prc_tau(histz.data(), hist.data(), PRC_NHISTORY, P.Omegam, P.Omegab, P.h);
   printf("\n\n tau = %f", tau);
-  // WriteHistory (io_d2z.C:284-314), first two columns
   printf("\n Writing ionization history...");
   std::string hname = std::string(CL.Basename) + ".history";
   FILE* fh = fopen(hname.c_str(), "w");
@@ -315,8 +366,11 @@ int main(int argc, char* argv[]) {
     printf("\n File %s could not be opened\n\n", hname.c_str());
     return 1;
   }
-  for (int i = 0; i < PRC_NHISTORY; i++) fprintf(fh, "%e %e\n", histz[i], hist[i]);
+  for (int i = 0; i < PRC_NHISTORY; i++)
+    fprintf(fh, "%e %e %e %e\n", histz[i], hist[i], prc_f2f_eval(&fct, histz[i]),
+            prc_fcoll(histz[i], P.zInit, P.Omegam, P.Omegal, P.w, tb.sigma_min));
   fclose(fh);
+  prc_f2f_free(&fct);
   prc_d2z_destroy(ctx);
   printf("\n\n");
   return 0;

@@ -33,7 +33,8 @@ from ._lib import (PRC_ARGMAX_NONE, PRC_FLAG_ARGMAX, PRC_FLAG_SIGMA_GRID, PRC_NH
 
 __all__ = ["Parameters", "CLParameters", "Tables", "read_parameter_file", "compute_tables",
            "Delta2Zreion", "delta2zreion", "PrcError", "PRC_ARGMAX_NONE", "PRC_NHISTORY",
-           "supported_sizes", "growth", "inverse_erfc", "tau"]
+           "supported_sizes", "growth", "inverse_erfc", "tau", "Float2FloatTable", "fcoll",
+           "chistory", "zvz_map"]
 
 
 @dataclass
@@ -150,6 +151,46 @@ def tau(history_z: np.ndarray, history: np.ndarray, omegam: float, omegab: float
     za = np.ascontiguousarray(history_z, np.float32)
     xa = np.ascontiguousarray(history, np.float32)
     return float(load().prc_tau(za.ctypes.data, xa.ctypes.data, len(za), omegam, omegab, h))
+
+
+class Float2FloatTable:
+    """Float2FloatTable (tables.C:9-38): f32 min, f32 max, i32 n, f32 table[n],
+    linear interpolation with spacing (max - min)/n."""
+
+    def __init__(self, path: str):
+        self._t = _lib.prc_f2f_table()
+        check(load().prc_f2f_load(path.encode(), ctypes.byref(self._t)))
+
+    def Float2Float(self, x: float) -> float:
+        return float(load().prc_f2f_eval(ctypes.byref(self._t), x))
+
+    def __del__(self):
+        try:
+            load().prc_f2f_free(ctypes.byref(self._t))
+        except Exception:
+            pass
+
+
+def fcoll(z: float, zInit: float, omegam: float, omegal: float, w: float, sigma_min: float) -> float:
+    """Press-Schechter collapsed fraction (cosmology.C:311-324)."""
+    return float(load().prc_fcoll(z, zInit, omegam, omegal, w, sigma_min))
+
+
+def chistory(table: Float2FloatTable, mfp, rmfp: float, zeta: float) -> np.ndarray:
+    """GetCHistory (bubblehistory_d2z.C:45-80): the MFP-corrected history."""
+    m = np.ascontiguousarray(mfp, np.float32)
+    out = np.zeros(_lib.PRC_NCHISTORY, np.float32)
+    check(load().prc_chistory(ctypes.byref(table._t), m.ctypes.data, len(m), rmfp, zeta, out.ctypes.data))
+    return out
+
+
+def zvz_map(history, chist) -> np.ndarray:
+    """CorrectHistory's z -> corrected z table (bubblehistory_d2z.C:314-326)."""
+    h = np.ascontiguousarray(history, np.float32)
+    c = np.ascontiguousarray(chist, np.float32)
+    out = np.zeros(PRC_NHISTORY, np.float32)
+    check(load().prc_zvz(h.ctypes.data, c.ctypes.data, out.ctypes.data))
+    return out
 
 
 def compute_tables(p: Parameters, cl: CLParameters) -> Tables:
@@ -329,6 +370,39 @@ class Delta2Zreion:
         check(L.prc_d2z_history(self._ctx, zp, on_dev, ctypes.c_void_p(counts.ctypes.data),
                                 ctypes.c_void_p(hist.ctypes.data), ctypes.c_void_p(hz.ctypes.data)))
         return counts, hist, hz
+
+    # ---------------------------------------------------------------- correction chain
+    def bubble_mfp(self, zreion, history, box_mpc: float, n_x: int = _lib.PRC_NX_MFP,
+                   n_skewers: int = _lib.PRC_NSKEWERS):
+        """GetBubbleMFP (bubblehistory_d2z.C:82-252): (mfp, mfp_x, dfdmfp)."""
+        z = np.ascontiguousarray(zreion, np.float32)
+        h = np.ascontiguousarray(history, np.float32)
+        s = _lib.prc_mfp_setup(self.N, box_mpc, n_x, n_skewers)
+        mfp = np.zeros(n_x, np.float32)
+        mfp_x = np.zeros(n_x, np.float32)
+        dfd = np.zeros(_lib.PRC_NMFP * n_x, np.float32)
+        check(load().prc_d2z_bubble_mfp(self._ctx, ctypes.byref(s), _host_ptr(z, np.float32, self.n3),
+                                        h.ctypes.data, mfp.ctypes.data, mfp_x.ctypes.data, dfd.ctypes.data))
+        return mfp, mfp_x, dfd
+
+    def correct(self, zreion, zvz):
+        """CorrectHistory's per-cell map, in place (host array or CUDA tensor)."""
+        zv = np.ascontiguousarray(zvz, np.float32)
+        if _is_torch(zreion):
+            check(load().prc_d2z_correct(self._ctx, zv.ctypes.data, _dev_ptr(zreion.reshape(-1), "float32", self.n3), 1))
+        else:
+            check(load().prc_d2z_correct(self._ctx, zv.ctypes.data, _host_ptr(zreion, np.float32, self.n3), 0))
+        return zreion
+
+    def correct_history(self, zreion, fcoll_table: str, box_mpc: float, rmfp: float, zeta: float,
+                        n_x: int = _lib.PRC_NX_MFP, n_skewers: int = _lib.PRC_NSKEWERS):
+        """main_d2z.C:76-87 on a host zreion grid, in place: GetHistory,
+        GetBubbleMFP, GetCHistory, CorrectHistory.  Returns (mfp, chistory)."""
+        _, hist, _ = self.history(zreion)
+        mfp, _, _ = self.bubble_mfp(zreion, hist, box_mpc, n_x, n_skewers)
+        ch = chistory(Float2FloatTable(fcoll_table), mfp, rmfp, zeta)
+        self.correct(zreion, zvz_map(hist, ch))
+        return mfp, ch
 
     # ---------------------------------------------------------------- adjoint
     def backward(self, dL_dz, argmax, dL_ddelta=None, want_dB: bool = True):

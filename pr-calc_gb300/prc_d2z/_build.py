@@ -30,7 +30,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCLUDE]
 
 CU_LIB = ["d2z_capi.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu", "inst_e.cu", "d2z_noalloc.cu"]
-CPP_LIB = ["errors.cpp", "cosmo.cpp"]
+CPP_LIB = ["errors.cpp", "cosmo.cpp", "history.cpp"]
 CPP_EXE = ["main_d2z.cpp"]
 
 

@@ -31,6 +31,8 @@ EXPORTS = [
     "prc_d2z_supported", "prc_d2z_create", "prc_d2z_forward", "prc_d2z_smooth", "prc_d2z_history",
     "prc_d2z_backward", "prc_d2z_last_timing", "prc_d2z_last_launches", "prc_d2z_profile",
     "prc_d2z_profile_read", "prc_d2z_destroy", "prc_d2z_forward_static",
+    "prc_f2f_load", "prc_f2f_eval", "prc_f2f_free", "prc_deltac", "prc_fcoll", "prc_d2z_bubble_mfp",
+    "prc_chistory", "prc_zvz", "prc_d2z_correct",
     "prc_last_error",
 ]
 
@@ -67,6 +69,21 @@ class prc_d2z_desc(ctypes.Structure):
                 ("radius_batch", ctypes.c_int), ("flags", ctypes.c_int), ("stream", ctypes.c_void_p)]
 
 
+class prc_f2f_table(ctypes.Structure):
+    _fields_ = [("minval", ctypes.c_float), ("maxval", ctypes.c_float), ("delta", ctypes.c_float),
+                ("n", ctypes.c_int), ("table", ctypes.POINTER(ctypes.c_float))]
+
+
+class prc_mfp_setup(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("box_mpc", ctypes.c_float), ("n_x", ctypes.c_int),
+                ("n_skewers", ctypes.c_int)]
+
+
+PRC_NCHISTORY = 10000
+PRC_NX_MFP = 1000
+PRC_NMFP = 200
+PRC_NSKEWERS = 20000
+
 _lib = None
 
 
@@ -100,10 +117,28 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_d2z_profile.argtypes = [vp, c_int]
     L.prc_d2z_forward_static.argtypes = [c_int, c_int, c_double, vp, vp, c_double, c_double, vp, vp, vp, vp]
     L.prc_d2z_profile_read.argtypes = [vp, P(c_double), P(ctypes.c_longlong)]
+    L.prc_f2f_load.argtypes = [ctypes.c_char_p, P(prc_f2f_table)]
+    L.prc_f2f_eval.argtypes = [P(prc_f2f_table), c_float]
+    L.prc_f2f_eval.restype = c_float
+    L.prc_f2f_free.argtypes = [P(prc_f2f_table)]
+    L.prc_f2f_free.restype = None
+    L.prc_deltac.argtypes = [c_float] * 4 + [P(c_float)]
+    L.prc_deltac.restype = c_float
+    L.prc_fcoll.argtypes = [c_float] * 6
+    L.prc_fcoll.restype = c_float
+    L.prc_d2z_bubble_mfp.argtypes = [vp, P(prc_mfp_setup), vp, vp, vp, vp, vp]
+    L.prc_chistory.argtypes = [P(prc_f2f_table), vp, c_int, c_float, c_float, vp]
+    L.prc_zvz.argtypes = [vp, vp, vp]
+    L.prc_d2z_correct.argtypes = [vp, vp, vp, c_int]
     for name in EXPORTS:
+        if name in ("prc_f2f_free",):
+            continue
         getattr(L, name).restype = getattr(L, name).restype or c_int
     L.prc_growth.restype = c_float
     L.prc_tau.restype = c_float
+    L.prc_f2f_eval.restype = c_float
+    L.prc_deltac.restype = c_float
+    L.prc_fcoll.restype = c_float
     L.prc_last_error.restype = ctypes.c_char_p
     _lib = L
     return L

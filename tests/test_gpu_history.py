@@ -1,0 +1,85 @@
+"""GPU parts of the history-correction chain (skewer walks, per-cell map) and
+the drop-in executable end to end."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import prc_d2z
+from oracle import history_ref as hr
+from prc_d2z import fields
+
+pytestmark = pytest.mark.gpu
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+H_ = 0.68
+
+
+def _zreion(N=32, seed=5, zeta=30.0):
+    box = 1.5 * N
+    p = prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box)
+    cl = prc_d2z.CLParameters(Rmax=0.4 * box, zeta=zeta, M_min=1.47e9)
+    delta = fields.gaussian_field(N, box, seed=seed)
+    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl)
+    z, _, _ = ctx.forward(delta)
+    return ctx, z, float(np.float32(box) / np.float32(H_)), delta, p, cl
+
+
+def test_bubble_mfp_matches_the_oracle():
+    ctx, z, box_mpc, *_ = _zreion()
+    _, hist, _ = ctx.history(z)
+    mfp, mfp_x, dfd = ctx.bubble_mfp(z, hist, box_mpc, n_x=16, n_skewers=48)
+    mo, mxo, dfo = hr.bubble_mfp(z, hist, box_mpc, 16, 48)
+    np.testing.assert_array_equal(mfp, mo)
+    np.testing.assert_array_equal(mfp_x, mxo)
+    np.testing.assert_array_equal(dfd, dfo)
+    ctx.close()
+
+
+def test_correct_matches_the_oracle(tmp_path):
+    ctx, z, box_mpc, *_ = _zreion(seed=6)
+    _, hist, _ = ctx.history(z)
+    ch = np.minimum(np.cumsum(np.full(10000, 1.2e-4, np.float32), dtype=np.float32), 1).astype(np.float32)
+    ch[0] = 0
+    zv = prc_d2z.zvz_map(hist, ch)
+    zc = ctx.correct(z.copy(), zv)
+    np.testing.assert_array_equal(zc, hr.correct(z, zv))
+    ctx.close()
+
+
+def test_executable_end_to_end(tmp_path):
+    """delta2zreion with the reference's command line and files."""
+    exe = os.path.join(REPO, "pr-calc_gb300", "bin", "delta2zreion")
+    N, box = 32, 48.0
+    delta = fields.gaussian_field(N, box, seed=7)
+    delta.tofile(tmp_path / "delta")
+    smin = prc_d2z.compute_tables(prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box),
+                                  prc_d2z.CLParameters(Rmax=20.0, zeta=30.0, M_min=1.47e9)).sigma_min
+    z = np.linspace(0.0, 50.0, 2001)
+    with open(tmp_path / "fcoll_table.tab", "wb") as fh:
+        np.array([0.0, 50.0], np.float32).tofile(fh)
+        np.array([len(z)], np.int32).tofile(fh)
+        np.array([hr.fcoll(v, 0.31, 0.69, -1.0, smin) for v in z], np.float32).tofile(fh)
+    (tmp_path / "param.d2z").write_text(
+        "# cosmology\nOmegam 0.31\nOmegal 0.69\nOmegab 0.049\nh 0.68\nns 0.965\nsigma8 0.81\nw -1\n"
+        f"BoxSize {box}\nN {N}\nzInit 0\nDeltaFile delta\nRmin 2\nNscales 10\nBogus 3\n")
+    r = subprocess.run([exe, "param.d2z", "-f", "run", "-m", "1.47e9", "-z", "30", "-r", "20", "-v", "-e"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Tag 'Bogus' not allowed" in r.stdout
+    assert "tau =" in r.stdout
+    used = (tmp_path / "param.d2z-usedvalues").read_text()
+    assert "Nscales" in used and "Bogus" not in used
+    out = tmp_path / "output"
+    zfile = np.fromfile(out / "run.zreion", np.float32).reshape(N, N, N)
+    # the same chain through the Python API
+    p = prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box)
+    cl = prc_d2z.CLParameters(Rmax=20.0, zeta=30.0, M_min=1.47e9)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl) as ctx:
+        zr, _, _ = ctx.forward(delta)
+        ctx.correct_history(zr, str(tmp_path / "fcoll_table.tab"), float(np.float32(box) / np.float32(0.68)),
+                            20.0, 30.0)
+    np.testing.assert_array_equal(zfile, zr)
+    hist = np.loadtxt(out / "run.history")
+    assert hist.shape == (100000, 4)
+    assert (out / "run.mfp").exists() and (out / "run.mfppdf").stat().st_size == 8 + 16 + 4 * 200 * 1000
