@@ -40,7 +40,9 @@ METRIC = "zreion cell*radii/s at 512^3 (64 radii)"
 UNIT = "cell*radii/s"
 N_DEF, BOX, NR, RMIN_CELLS, RMAX, H_ = 512, 600.0, 64, 2.0, 60.0, 0.68
 MMIN_MSUN = 1e9 / H_
-ZETA = 30.0          # calibrated: x_i(z=8) ~ 0.5 at seed 1
+# zeta from prc_d2z.calibrate: raw zreion with x_i(z=8) = 0.5 at seed 1
+ZETA = 80.5404       # 512^3, 600 Mpc/h, 64 radii to 60 Mpc/h
+ZETA_BATCH = 81.6855 # 256^3, 384 Mpc/h (1.5 Mpc/h cells), 48 radii to 60 Mpc/h
 CPU_SAMPLE_RADII = 4
 
 
@@ -313,6 +315,128 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(out), flush=True)
 
 
+def _cfg_box(N, nr, seed, zeta, box=None, rmax=RMAX):
+    import prc_d2z
+    box = box if box is not None else 1.5 * N
+    p = prc_d2z.Parameters(N=N, Nscales=nr, BoxSize=box, Rmin=RMIN_CELLS)
+    cl = prc_d2z.CLParameters(Rmax=rmax, zeta=zeta, M_min=MMIN_MSUN)
+    t = prc_d2z.compute_tables(p, cl)
+    return dict(N=N, box_mpc=float(np.float32(box) / np.float32(H_)), radii_mpc=t.radii_mpc,
+                barrier_b=t.barrier_b, barrier_a=t.barrier_a, growth_init=t.DInit), box
+
+
+def run_batched(args):
+    """96 realisations, grids 64/96/128/192/256 at 1.5 Mpc/h cells, 24-48 radii
+    each: per-box loop of the plain path vs one captured-graph batch launch."""
+    import torch
+
+    import prc_d2z
+    from prc_d2z import fields
+    rng = np.random.default_rng(2024)
+    sizes = [64] * 20 + [96] * 19 + [128] * 19 + [192] * 19 + [256] * 19
+    rng.shuffle(sizes)
+    nrs = rng.integers(24, 49, len(sizes))
+    boxes, deltas = [], []
+    for i, (N, nr) in enumerate(zip(sizes, nrs)):
+        b, box = _cfg_box(int(N), int(nr), 1000 + i, ZETA_BATCH)
+        boxes.append(b)
+        deltas.append(fields.gaussian_field(int(N), box, seed=1000 + i, backend="torch").contiguous())
+    work = sum(b["N"] ** 3 * len(b["radii_mpc"]) for b in boxes)
+    outs_loop = [torch.empty_like(d) for d in deltas]
+    outs_batch = [torch.empty_like(d) for d in deltas]
+    ctxs = [prc_d2z.Delta2Zreion(b["N"], b["box_mpc"], b["radii_mpc"], b["barrier_b"], b["barrier_a"],
+                                 b["growth_init"], argmax=False) for b in boxes]
+
+    def loop():
+        for c, d, o in zip(ctxs, deltas, outs_loop):
+            c.forward(d, zreion=o, want_argmax=False)
+
+    batch = prc_d2z.Batch(boxes, n_streams=args.streams)
+
+    def batched():
+        batch.forward(deltas, outs_batch, use_graph=True)
+
+    res = {}
+    for name, fn in (("loop", loop), ("batched", batched)):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(0) as clk:
+            e0.record()
+            for _ in range(args.steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+        res[name] = (e0.elapsed_time(e1) / args.steps, clk.summary())
+    same = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_batch))
+    ms_loop, ms_b = res["loop"][0], res["batched"][0]
+    print(json.dumps({
+        "metric": "batched zreion cell*radii/s (96 boxes, 64-256^3, 24-48 radii)", "value": work / (ms_b * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Philox4x32-10 + BBKS, seeds 1000..1095)",
+        "config": {"workload": "batched: 96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
+                               "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
+                   "streams": args.streams, "graph": True},
+        "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3)},
+        "speedup_vs_loop": ms_loop / ms_b, "identical_to_loop": bool(same),
+        "gpu_launches": batch.launches(), "clocks": res["batched"][1]}), flush=True)
+    batch.close()
+    for c in ctxs:
+        c.close()
+
+
+def run_adjoint(args):
+    """Adjoint at N^3 with 64 radii: loss = mean((z - z_t)^2), z_t from seed 2;
+    forward (with argmax) and backward timed; ratio t_bwd / t_fwd."""
+    import torch
+
+    import prc_d2z
+    from prc_d2z import fields
+    N = args.n
+    box = BOX * N / N_DEF
+    p = prc_d2z.Parameters(N=N, Nscales=NR, BoxSize=box, Rmin=RMIN_CELLS)
+    cl = prc_d2z.CLParameters(Rmax=RMAX, zeta=ZETA, M_min=MMIN_MSUN)
+    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=args.batch, argmax=True)
+    delta = fields.gaussian_field(N, box, seed=1, backend="torch").contiguous()
+    target = fields.gaussian_field(N, box, seed=2, backend="torch").contiguous()
+    zt, _, _ = ctx.forward(target, want_argmax=False)
+    zt = zt.clone()
+    z = torch.empty_like(delta)
+    am = torch.empty(delta.shape, dtype=torch.uint8, device=delta.device)
+    grad = torch.empty_like(delta)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(args.warmup):
+        ctx.forward(delta, zreion=z, argmax=am)
+        g = (2.0 / N ** 3) * (z - zt)
+        ctx.backward(g, am, dL_ddelta=grad)
+    torch.cuda.synchronize()
+    tf = tb = 0.0
+    for _ in range(args.steps):
+        ev[0].record()
+        ctx.forward(delta, zreion=z, argmax=am)
+        ev[1].record()
+        g = (2.0 / N ** 3) * (z - zt)
+        ev[2].record()
+        ctx.backward(g, am, dL_ddelta=grad)
+        ev[3].record()
+        torch.cuda.synchronize()
+        tf += ev[0].elapsed_time(ev[1])
+        tb += ev[2].elapsed_time(ev[3])
+    tf /= args.steps
+    tb /= args.steps
+    print(json.dumps({
+        "metric": f"adjoint/forward time ratio at {N}^3 (64 radii)", "value": tb / tf, "unit": "ratio",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tf + tb,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Philox4x32-10 + BBKS, field seed 1, target seed 2)",
+        "config": {"workload": f"adjoint {N}^3, {box:g} Mpc/h, 64 radii, loss mean((z-z_t)^2)", "zeta": ZETA},
+        "forward_ms": tf, "backward_ms": tb,
+        "backward_cell_radii_per_s": N ** 3 * NR / (tb * 1e-3)}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,7 +447,15 @@ def main():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--ref-radii", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
+    ap.add_argument("--streams", type=int, default=4)
     args = ap.parse_args()
+    if args.workload == "batched" and args.impl == "ours":
+        run_batched(args)
+        return
+    if args.workload == "adjoint" and args.impl == "ours":
+        run_adjoint(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

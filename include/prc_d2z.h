@@ -105,6 +105,10 @@ typedef struct {
   void*         stream;           /* cudaStream_t; NULL = default stream        */
 } prc_d2z_desc;
 
+/* Replaces the barrier table of a context (same radii): B_r and A as in the
+ * descriptor.  For parameter scans (e.g. zeta) without a new workspace. */
+int prc_d2z_set_barrier(prc_d2z_ctx* ctx, const double* barrier_b, double barrier_a);
+
 /* 1 if N has a compiled FFT plan, else 0. */
 int prc_d2z_supported(int N);
 
@@ -201,6 +205,20 @@ int prc_d2z_last_timing(prc_d2z_ctx* ctx, float* ms3);
 
 /* Kernel launches issued by the last forward/backward call. */
 int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
+
+/* ---- batches of boxes ------------------------------------------------------
+ * Many independent boxes (realisations), possibly of different grid sizes:
+ * one workspace per box, boxes spread over n_streams streams, and with
+ * use_graph = 1 the kernels of all boxes captured once into a CUDA graph and
+ * replayed with one launch per call (re-captured when the pointers change).
+ * delta, zreion (and argmax, nullable) are arrays of n_boxes device pointers.
+ * No reference counterpart: the reference processes one box per run. */
+typedef struct prc_d2z_batch prc_d2z_batch;
+int prc_d2z_batch_create(int n_boxes, const prc_d2z_desc* descs, int n_streams, prc_d2z_batch** out);
+int prc_d2z_batch_forward(prc_d2z_batch* batch, const float* const* delta, float* const* zreion,
+                          uint8_t* const* argmax, int use_graph);
+int prc_d2z_batch_launches(prc_d2z_batch* batch, int* n);
+int prc_d2z_batch_destroy(prc_d2z_batch* batch);
 
 /* Per-kernel timing: with profiling enabled every launch is bracketed by CUDA
  * events on the context's stream and the totals accumulate per kernel kind

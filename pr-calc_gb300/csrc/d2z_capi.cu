@@ -13,6 +13,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/prc_d2z.h"
@@ -281,7 +282,7 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
   if (mode == TM_WIN || mode == TM_ACC)
     for (int b = 0; b < nb; ++b) a.kr[b] = c->kr[r0 + b];
   const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
-  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : c->ksl.occ_tile;
+  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : (mode == TM_WIN) ? c->ksl.occ_tile_win : c->ksl.occ_tile;
   dim3 grid(grid_for(tiles, 1, occ, c->sms), gy, 1);
   const int kind = mode == TM_FWD ? PRC_KIND_COL_FWD
                  : mode == TM_INV ? PRC_KIND_COL_INV
@@ -322,6 +323,82 @@ void forward_r2c(prc_d2z_ctx* c, const float* d_delta) {
   run_tile(c, TM_FWD, mseg(c, S, S, false), qseg(c, Qt, Q, true), 1);
   // x pass: main in place; Nyquist Q in place
   run_tile(c, TM_FWD, mseg(c, S, S, true), qseg(c, Q, Q, false), 1);
+}
+
+// All radius sweeps of a forward call, kernels only (no copies, events or
+// synchronisation), so that the same sequence can be captured into a graph.
+void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig) {
+  const int N = c->N, H = c->H;
+  const long long NN = c->NN;
+  for (int r0 = 0; r0 < c->nr; r0 += c->B) {
+    const int nb = (c->nr - r0 < c->B) ? c->nr - r0 : c->B;
+    SweepArgs sa;
+    memset(&sa, 0, sizeof(sa));
+    sa.slots = c->slots;
+    sa.slot_stride = c->slot_f2;
+    sa.tw = c->tw;
+    sa.zreion = d_z;
+    sa.argmax = d_am;
+    sa.sig_acc = sig;
+    sa.nb = nb;
+    sa.r0 = r0;
+    sa.first = (r0 == 0);
+    sa.as = c->as;
+    for (int b = 0; b < nb; ++b) sa.cb[b] = c->cb[r0 + b];
+    float2* U = c->slots;
+    // window + inverse x pass: spectrum -> slots (Nyquist plane transposed)
+    run_tile(c, TM_WIN, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1, nb, r0);
+    // inverse y pass of every slot, in place
+    run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), nb);
+    {
+      Prof pf(c, PRC_KIND_C2R_Z);
+      c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, sa);
+    }
+    c->launches++;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ batches
+// Many boxes of (possibly) different sizes: one context per box, boxes spread
+// round-robin over a few streams, optionally all captured into one CUDA graph
+// and replayed with a single launch.
+struct prc_d2z_batch {
+  int n = 0, dev = 0;
+  std::vector<prc_d2z_ctx*> ctx;
+  std::vector<cudaStream_t> streams;
+  cudaStream_t origin = nullptr;
+  std::vector<cudaEvent_t> ev;  // fork + one join per stream
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void*> key;  // pointers the graph was captured with
+};
+
+namespace {
+
+void batch_free(prc_d2z_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto* c : b->ctx) prc_d2z_destroy(c);
+  for (auto e : b->ev) cudaEventDestroy(e);
+  for (auto s : b->streams) cudaStreamDestroy(s);
+  if (b->origin) cudaStreamDestroy(b->origin);
+}
+
+void batch_enqueue(prc_d2z_batch* b, const float* const* delta, float* const* zreion, uint8_t* const* argmax) {
+  cudaEventRecord(b->ev[0], b->origin);
+  for (auto s : b->streams) cudaStreamWaitEvent(s, b->ev[0], 0);
+  for (int i = 0; i < b->n; ++i) {
+    prc_d2z_ctx* c = b->ctx[i];
+    c->launches = 0;
+    forward_r2c(c, delta[i]);
+    enqueue_sweeps(c, zreion[i], argmax ? argmax[i] : nullptr, nullptr);
+  }
+  for (size_t k = 0; k < b->streams.size(); ++k) {
+    cudaEventRecord(b->ev[1 + k], b->streams[k]);
+    cudaStreamWaitEvent(b->origin, b->ev[1 + k], 0);
+  }
 }
 
 }  // namespace
@@ -441,32 +518,7 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
   PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
   forward_r2c(c, d_delta);
   PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
-  for (int r0 = 0; r0 < c->nr; r0 += c->B) {
-    const int nb = (c->nr - r0 < c->B) ? c->nr - r0 : c->B;
-    SweepArgs sa;
-    memset(&sa, 0, sizeof(sa));
-    sa.slots = c->slots;
-    sa.slot_stride = c->slot_f2;
-    sa.tw = c->tw;
-    sa.zreion = d_z;
-    sa.argmax = d_am;
-    sa.sig_acc = want_sig ? c->sig : nullptr;
-    sa.nb = nb;
-    sa.r0 = r0;
-    sa.first = (r0 == 0);
-    sa.as = c->as;
-    for (int b = 0; b < nb; ++b) sa.cb[b] = c->cb[r0 + b];
-    float2* U = c->slots;
-    // window + inverse x pass: spectrum -> slots (Nyquist plane transposed)
-    run_tile(c, TM_WIN, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1, nb, r0);
-    // inverse y pass of every slot, in place
-    run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), nb);
-    {
-      Prof pf(c, PRC_KIND_C2R_Z);
-      c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, sa);
-    }
-    c->launches++;
-  }
+  enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr);
   PRC_CU(cudaGetLastError(), "kernel launch");
   PRC_CU(cudaEventRecord(c->ev[2], c->st), "event");
   if (!out_on_device) {
@@ -725,6 +777,118 @@ int prc_d2z_correct(prc_d2z_ctx* c, const float* zvz, float* zreion, int on_devi
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   cudaFree(d_zvz);
   if (e != cudaSuccess) return cuda_fail(e, "prc_d2z_correct");
+  return PRC_OK;
+}
+
+int prc_d2z_set_barrier(prc_d2z_ctx* c, const double* barrier_b, double barrier_a) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!barrier_b || !(barrier_a > 0)) return prc_fail(PRC_ERR_INVALID, "prc_d2z_set_barrier: bad argument");
+  const double n3 = (double)c->NN * c->N;
+  c->A = barrier_a;
+  c->as = (float)(barrier_a / n3);
+  for (int r = 0; r < c->nr; ++r) {
+    c->Bb[r] = barrier_b[r];
+    c->cb[r] = (float)(barrier_a * barrier_b[r] - 1.0);
+  }
+  return PRC_OK;
+}
+
+int prc_d2z_batch_create(int n_boxes, const prc_d2z_desc* descs, int n_streams, prc_d2z_batch** out) {
+  if (!descs || !out || n_boxes < 1) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_create: bad argument");
+  if (n_streams < 1) n_streams = 1;
+  if (n_streams > n_boxes) n_streams = n_boxes;
+  *out = nullptr;
+  prc_d2z_batch* b = new prc_d2z_batch();
+  b->n = n_boxes;
+  cudaError_t e = cudaGetDevice(&b->dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
+  for (int k = 0; k < n_streams && e == cudaSuccess; ++k) {
+    cudaStream_t s;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) b->streams.push_back(s);
+  }
+  for (int k = 0; k <= n_streams && e == cudaSuccess; ++k) {
+    cudaEvent_t ev;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->ev.push_back(ev);
+  }
+  if (e != cudaSuccess) {
+    batch_free(b);
+    delete b;
+    return cuda_fail(e, "prc_d2z_batch_create");
+  }
+  // larger boxes first, so that the round-robin spreads the work evenly
+  std::vector<int> order(n_boxes);
+  for (int i = 0; i < n_boxes; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return descs[x].N > descs[y].N; });
+  b->ctx.assign(n_boxes, nullptr);
+  for (int k = 0; k < n_boxes; ++k) {
+    const int i = order[k];
+    prc_d2z_desc d = descs[i];
+    d.stream = b->streams[k % n_streams];
+    int st = prc_d2z_create(&d, &b->ctx[i]);
+    if (st != PRC_OK) {
+      batch_free(b);
+      delete b;
+      return st;
+    }
+  }
+  *out = b;
+  return PRC_OK;
+}
+
+int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* const* zreion,
+                          uint8_t* const* argmax, int use_graph) {
+  if (!b || !delta || !zreion) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null argument");
+  for (int i = 0; i < b->n; ++i)
+    if (!delta[i] || !zreion[i]) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null pointer for box %d", i);
+  int cur = -1;
+  PRC_CU(cudaGetDevice(&cur), "cudaGetDevice");
+  if (cur != b->dev) PRC_CU(cudaSetDevice(b->dev), "cudaSetDevice");
+  if (!use_graph) {
+    batch_enqueue(b, delta, zreion, argmax);
+    PRC_CU(cudaGetLastError(), "prc_d2z_batch_forward");
+    PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
+    return PRC_OK;
+  }
+  std::vector<const void*> key;
+  for (int i = 0; i < b->n; ++i) {
+    key.push_back(delta[i]);
+    key.push_back(zreion[i]);
+    key.push_back(argmax ? argmax[i] : nullptr);
+  }
+  if (!b->exec || key != b->key) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    PRC_CU(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal), "begin capture");
+    batch_enqueue(b, delta, zreion, argmax);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->origin, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    b->graph = g;
+    PRC_CU(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    b->key = key;
+  }
+  PRC_CU(cudaGraphLaunch(b->exec, b->origin), "graph launch");
+  PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
+  return PRC_OK;
+}
+
+int prc_d2z_batch_launches(prc_d2z_batch* b, int* n) {
+  if (!b || !n) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_launches: null argument");
+  int t = 0;
+  for (auto* c : b->ctx) t += c->launches;
+  *n = t;
+  return PRC_OK;
+}
+
+int prc_d2z_batch_destroy(prc_d2z_batch* b) {
+  if (!b) return PRC_OK;
+  batch_free(b);
+  delete b;
   return PRC_OK;
 }
 

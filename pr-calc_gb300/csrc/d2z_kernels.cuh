@@ -87,7 +87,8 @@ template <int N> struct TK {
   static_assert(H % T == 0 && N % T == 0 && T % 2 == 0, "tile width");
   static constexpr int THREADS = T * G;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
-  static constexpr int smem_f2 = TW + 2 * N * T;       // twiddles + two tiles
+  static constexpr int smem_f2 = TW + N * T;            // twiddles + one tile
+  static constexpr int smem2_f2 = TW + 2 * N * T;       // twiddles + two tiles (TM_WIN)
   // resident CTAs per SM the register budget is sized for; the accumulate
   // mode keeps E more complex values per thread
   static constexpr int MINB = THREADS >= 512 ? 2 : (THREADS >= 256 ? 3 : 4);

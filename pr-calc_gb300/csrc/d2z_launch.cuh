@@ -9,7 +9,8 @@ namespace prc {
 template <int N> struct Launchers {
   using TT = TK<N>;
   using LL = LK<N>;
-  static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);
+  static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);    // one tile
+  static constexpr size_t TS2 = (size_t)TT::smem2_f2 * sizeof(float2);  // two tiles (TM_WIN)
   static constexpr size_t LS = (size_t)LL::smem_f2 * sizeof(float2);
 
   template <class F> static cudaError_t smem(F fn, size_t bytes) {
@@ -28,13 +29,14 @@ template <int N> struct Launchers {
     cudaError_t e;
     if ((e = smem(tf, TS)) != cudaSuccess) return e;
     if ((e = smem(ti, TS)) != cudaSuccess) return e;
-    if ((e = smem(tw, TS)) != cudaSuccess) return e;
+    if ((e = smem(tw, TS2)) != cudaSuccess) return e;
     if ((e = smem(ta, TS)) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile, tw, TT::THREADS, TS)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile, ti, TT::THREADS, TS)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile_win, tw, TT::THREADS, TS2)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_acc, ta, TT::THREADS, TS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r, &k_c2r_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
@@ -49,7 +51,7 @@ template <int N> struct Launchers {
     switch (mode) {
       case TM_FWD: k_tile<N, TM_FWD><<<grid, TT::THREADS, TS, st>>>(a); break;
       case TM_INV: k_tile<N, TM_INV><<<grid, TT::THREADS, TS, st>>>(a); break;
-      case TM_WIN: k_tile<N, TM_WIN><<<grid, TT::THREADS, TS, st>>>(a); break;
+      case TM_WIN: k_tile<N, TM_WIN><<<grid, TT::THREADS, TS2, st>>>(a); break;
       default: k_tile<N, TM_ACC><<<grid, TT::THREADS, TS, st>>>(a); break;
     }
   }

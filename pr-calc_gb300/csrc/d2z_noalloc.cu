@@ -164,7 +164,7 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     a.nb = 1;
     if (mode == TM_WIN) a.kr[0] = (float)(2.0 * M_PI / box_mpc * radii_mpc[r]);
     const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
-    ks.tile(ks, mode, dim3(grid_of(tiles, ks.occ_tile, sms), 1, 1), st, a);
+    ks.tile(ks, mode, dim3(grid_of(tiles, mode == TM_WIN ? ks.occ_tile_win : ks.occ_tile, sms), 1, 1), st, a);
   };
   // forward R2C: z lines, then y and x column passes (Nyquist plane via the
   // transposed scratch after it in the spectrum region)

@@ -34,7 +34,7 @@ from ._lib import (PRC_ARGMAX_NONE, PRC_FLAG_ARGMAX, PRC_FLAG_SIGMA_GRID, PRC_NH
 __all__ = ["Parameters", "CLParameters", "Tables", "read_parameter_file", "compute_tables",
            "Delta2Zreion", "delta2zreion", "PrcError", "PRC_ARGMAX_NONE", "PRC_NHISTORY",
            "supported_sizes", "growth", "inverse_erfc", "tau", "Float2FloatTable", "fcoll",
-           "chistory", "zvz_map"]
+           "chistory", "zvz_map", "Batch"]
 
 
 @dataclass
@@ -334,6 +334,12 @@ class Delta2Zreion:
                                _host_ptr(out, np.float32, self.n3), 0))
         return out
 
+    def set_barrier(self, barrier_b, barrier_a: float) -> None:
+        """New barrier table for the same radii (prc_d2z_set_barrier)."""
+        b = np.ascontiguousarray(barrier_b, np.float64)
+        check(load().prc_d2z_set_barrier(self._ctx, b.ctypes.data, float(barrier_a)))
+        self.barrier_b, self.barrier_a = b, float(barrier_a)
+
     def last_timing(self):
         ms = (ctypes.c_float * 3)()
         check(load().prc_d2z_last_timing(self._ctx, ms))
@@ -427,6 +433,69 @@ class Delta2Zreion:
                                      _host_ptr(a, np.uint8, self.n3), 0,
                                      _host_ptr(dL_ddelta, np.float32, self.n3), 0, dBp))
         return dL_ddelta, dB
+
+
+class Batch:
+    """Many boxes (any mix of supported grid sizes) run together: one
+    workspace per box, n_streams CUDA streams, and with use_graph the kernels
+    of all boxes captured into one CUDA graph (prc_d2z_batch_*).
+
+    boxes: list of dicts with the Delta2Zreion arguments (N, box_mpc,
+    radii_mpc, barrier_b, barrier_a, growth_init, radius_batch)."""
+
+    def __init__(self, boxes, n_streams: int = 4):
+        L = load()
+        self.n = len(boxes)
+        self.N = [int(b["N"]) for b in boxes]
+        self._keep = []
+        descs = (_lib.prc_d2z_desc * self.n)()
+        for i, b in enumerate(boxes):
+            R = np.ascontiguousarray(b["radii_mpc"], np.float64)
+            B = np.ascontiguousarray(b["barrier_b"], np.float64)
+            self._keep += [R, B]
+            d = descs[i]
+            d.N = int(b["N"])
+            d.n_radii = len(R)
+            d.box_mpc = float(b["box_mpc"])
+            d.radii_mpc = R.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            d.barrier_b = B.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            d.barrier_a = float(b["barrier_a"])
+            d.growth_init = float(b.get("growth_init", 1.0))
+            d.radius_batch = int(b.get("radius_batch", 0))
+            d.flags = 0
+        self._b = ctypes.c_void_p()
+        check(L.prc_d2z_batch_create(self.n, descs, int(n_streams), ctypes.byref(self._b)))
+
+    def forward(self, deltas, zreions, argmaxes=None, use_graph: bool = True):
+        """deltas/zreions (/argmaxes): lists of contiguous CUDA tensors."""
+        L = load()
+        n = self.n
+        dp = (ctypes.c_void_p * n)(*[_dev_ptr(d.reshape(-1), "float32", self.N[i] ** 3).value
+                                    for i, d in enumerate(deltas)])
+        zp = (ctypes.c_void_p * n)(*[_dev_ptr(z.reshape(-1), "float32", self.N[i] ** 3).value
+                                    for i, z in enumerate(zreions)])
+        ap = None
+        if argmaxes is not None:
+            ap = (ctypes.c_void_p * n)(*[_dev_ptr(a.reshape(-1), "uint8", self.N[i] ** 3).value
+                                        for i, a in enumerate(argmaxes)])
+        check(L.prc_d2z_batch_forward(self._b, dp, zp, ap, 1 if use_graph else 0))
+        return zreions
+
+    def launches(self) -> int:
+        n = ctypes.c_int()
+        check(load().prc_d2z_batch_launches(self._b, ctypes.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "_b", None) and self._b.value:
+            load().prc_d2z_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def delta2zreion(delta_lin, p: Parameters, cl: CLParameters, **kw):

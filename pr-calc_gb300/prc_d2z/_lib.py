@@ -32,7 +32,8 @@ EXPORTS = [
     "prc_d2z_backward", "prc_d2z_last_timing", "prc_d2z_last_launches", "prc_d2z_profile",
     "prc_d2z_profile_read", "prc_d2z_destroy", "prc_d2z_forward_static",
     "prc_f2f_load", "prc_f2f_eval", "prc_f2f_free", "prc_deltac", "prc_fcoll", "prc_d2z_bubble_mfp",
-    "prc_chistory", "prc_zvz", "prc_d2z_correct",
+    "prc_chistory", "prc_zvz", "prc_d2z_correct", "prc_d2z_batch_create", "prc_d2z_batch_forward",
+    "prc_d2z_batch_launches", "prc_d2z_batch_destroy", "prc_d2z_set_barrier",
     "prc_last_error",
 ]
 
@@ -130,6 +131,11 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_chistory.argtypes = [P(prc_f2f_table), vp, c_int, c_float, c_float, vp]
     L.prc_zvz.argtypes = [vp, vp, vp]
     L.prc_d2z_correct.argtypes = [vp, vp, vp, c_int]
+    L.prc_d2z_batch_create.argtypes = [c_int, P(prc_d2z_desc), c_int, P(vp)]
+    L.prc_d2z_batch_forward.argtypes = [vp, P(vp), P(vp), P(vp), c_int]
+    L.prc_d2z_batch_launches.argtypes = [vp, P(c_int)]
+    L.prc_d2z_batch_destroy.argtypes = [vp]
+    L.prc_d2z_set_barrier.argtypes = [vp, vp, c_double]
     for name in EXPORTS:
         if name in ("prc_f2f_free",):
             continue
