@@ -1,0 +1,228 @@
+// d2z_cols.cuh — column passes with one lane per column (grids with N >= 32
+// and H a multiple of 16).
+//
+// A tile is 16 adjacent columns x N rows.  Thread (t, c) of a CTA of 16*G
+// threads holds rows t + G*m (m < E) of column c in registers: the 16 lanes of
+// a half-warp are the 16 columns of one row, so every global load and store
+// is a whole 128-byte row segment and the data go straight from HBM into the
+// FFT registers and back, with no shared-memory staging of the tile.  Only
+// the Stockham exchanges touch shared memory: row p of column c lives at
+// p*16 + c, so a half-warp always touches 16 consecutive words (no bank
+// conflict, no swizzle), and the CTA alternates between two exchange buffers
+// so that each exchange costs one barrier.  A warp holds the two FFT lanes t
+// and G - t (lanes 0 and G/2 share warp 0); their rows ix and N - ix have the
+// same |k|, so the window is evaluated once per mirror pair and handed over
+// with one shuffle.
+//
+// Modes as in k_tile: TM_FWD / TM_INV plain transforms (blockIdx.y selects a
+// slot; the next tile is loaded into registers while the current one is
+// transformed), TM_WIN (spectrum tile read once, then per radius: window,
+// inverse transform, store to the radius slot; the next tile's load is issued
+// during the last radius), TM_ACC (per radius: forward transform of the slot
+// tile, accumulate W_b times it; one read-modify-write of the output).
+#pragma once
+#include "d2z_kernels.cuh"
+
+namespace prc {
+
+template <int N> struct CCfg { static constexpr bool on = false; };
+template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
+template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
+template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
+template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; };
+template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
+template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; };
+
+template <int N> struct CK {
+  using P = typename CCfg<N>::P;
+  static constexpr int H = N / 2, T = 16, E = P::E, G = N / E, THREADS = T * G;
+  static_assert(PlanRun<P>::L == N, "column plan length");
+  static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
+  static constexpr int EH = E / 2;
+  static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
+  static constexpr int BUF = N * T;                     // one exchange buffer
+  static constexpr int smem_f2 = TW + 2 * BUF;
+  static constexpr int MINB = THREADS >= 512 ? 1 : (THREADS >= 256 ? 2 : 4);
+};
+
+// Two exchange buffers, column c: row p at p*16 + c.  Rows split as tp | cp
+// (disjoint bits) address as tp*16 + cp*16.
+template <int T> struct PPCol {
+  float2* b;
+  int other;  // offset to the other buffer
+  __device__ __forceinline__ int thread(int tp) const { return tp * T; }
+  __device__ __forceinline__ float2 get(int h, int cp) const { return b[h + cp * T]; }
+  __device__ __forceinline__ void put(int h, int cp, float2 v) const { b[h + cp * T] = v; }
+  __device__ __forceinline__ float2 get_pos(int p) const { return b[p * T]; }
+  __device__ __forceinline__ void put_pos(int p, float2 v) const { b[p * T] = v; }
+  __device__ __forceinline__ void flip() {
+    b += other;
+    other = -other;
+  }
+};
+
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a) {
+  using KK = CK<N>;
+  using P = typename KK::P;
+  constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, EH = KK::EH;
+  constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);
+  extern __shared__ float4 smem4[];
+  float2* tws = reinterpret_cast<float2*>(smem4);
+  __shared__ float s_kr[kMaxBatch];
+  if constexpr (MODE == TM_WIN || MODE == TM_ACC) stage_params(s_kr, a.kr);
+  PlanRun<P>::template fill<1>(tws, a.tw);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, c = lane & 15;
+  const int t = (lane < 16) ? wp : (wp == 0 ? G / 2 : G - wp);
+  PPCol<T> buf{tws + KK::TW + c, KK::BUF};
+  const CtaSync sync;
+  const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
+  const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;
+  const int tiles = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;
+
+  struct Where {
+    TileSeg sg;
+    int outer, tc;
+    long long off;
+  };
+  auto where = [&](int ti) {
+    Where w;
+    const bool sn = ti >= tiles0;
+    w.sg = sn ? a.seg[1] : a.seg[0];
+    const int tl = sn ? ti - tiles0 : ti;
+    w.outer = tl / w.sg.tpo;
+    w.tc = tl - w.outer * w.sg.tpo;
+    w.off = (long long)w.outer * w.sg.outer_stride + (long long)w.tc * T;
+    return w;
+  };
+  auto gload = [&](const float2* base, int rs, float2 (&v)[E]) {
+    const float2* p = base + (long long)t * rs + c;
+    const long long step = (long long)G * rs;
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = __ldg(p + m * step);
+  };
+  auto gstore = [&](const Where& w, float2* dst, const float2 (&v)[E]) {
+    if (w.sg.transpose) {
+      float2* q = dst + (long long)w.outer * w.sg.outer_stride + (long long)(w.tc * T + c) * N + t;
+#pragma unroll
+      for (int m = 0; m < E; ++m) q[G * m] = v[m];
+    } else {
+      float2* q = dst + w.off + (long long)t * w.sg.row_stride + c;
+      const long long step = (long long)G * w.sg.row_stride;
+#pragma unroll
+      for (int m = 0; m < E; ++m) q[m * step] = v[m];
+    }
+  };
+  // |k| of rows t + G*m, m <= E/2, of this thread's column (-1: k = 0)
+  auto kmag = [&](const Where& w, float (&kq)[EH + 1]) {
+    const int col = w.tc * T + c;
+    const int syz = w.sg.nyq ? fsq(col, N) + H * H : fsq(w.outer, N) + col * col;
+#pragma unroll
+    for (int m = 0; m <= EH; ++m) {
+      const int m2 = fsq(t + G * m, N) + syz;
+      kq[m] = (m2 == 0) ? -1.f : sqrtf((float)m2);
+    }
+  };
+  // W(|k| R_b) of all E rows: rows m > E/2 mirror rows of the partner lane
+  // (G - t, register E-1-m) or, in warp 0, of this lane (t = 0: E-m; t = G/2:
+  // E-1-m)
+  auto wvals = [&](const float (&kq)[EH + 1], float kr, float (&wv)[E]) {
+#pragma unroll
+    for (int m = 0; m <= EH; ++m) wv[m] = (kq[m] < 0.f) ? 0.f : tophat(kq[m] * kr);
+#pragma unroll
+    for (int m = EH + 1; m < E; ++m) {
+      const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
+      const float own = (t == 0) ? wv[E - m] : wv[E - 1 - m];
+      wv[m] = (wp == 0) ? own : o;
+    }
+  };
+
+  if constexpr (MODE == TM_FWD || MODE == TM_INV) {
+    float2 v[E], nx[E];
+    int ti = blockIdx.x;
+    if (ti < tiles) {
+      const Where w = where(ti);
+      gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
+    }
+    for (; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      const int tn = ti + gridDim.x;
+      if (tn < tiles) {
+        const Where wn = where(tn);
+        gload(wn.sg.in + wn.off + yoff, wn.sg.row_stride, nx);
+      }
+      PlanRun<P>::template run<INV, true>(v, buf, t, tws, sync);
+      gstore(w, w.sg.out + yoff, v);
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = nx[m];
+    }
+  } else if constexpr (MODE == TM_WIN) {
+    float2 raw[E];
+    int ti = blockIdx.x;
+    if (ti < tiles) {
+      const Where w = where(ti);
+      gload(w.sg.in + w.off, w.sg.row_stride, raw);
+    }
+    for (; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      float kq[EH + 1];
+      kmag(w, kq);
+      auto radius = [&](int b, bool last) {
+        float wv[E];
+        wvals(kq, s_kr[b], wv);
+        float2 v[E];
+#pragma unroll
+        for (int m = 0; m < E; ++m) v[m] = cscale(raw[m], wv[m]);
+        if (last) {
+          // raw and kq are dead: the next tile's loads overlap this radius
+          const int tn = ti + gridDim.x;
+          if (tn < tiles) {
+            const Where wn = where(tn);
+            gload(wn.sg.in + wn.off, wn.sg.row_stride, raw);
+          }
+        }
+        PlanRun<P>::template run<true, true>(v, buf, t, tws, sync);
+        gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
+      };
+      // the last radius is peeled so that kq's and raw's live ranges end before it
+      for (int b = 0; b < a.nb - 1; ++b) radius(b, false);
+      radius(a.nb - 1, true);
+    }
+  } else {  // TM_ACC (output never transposed)
+    for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      float kq[EH + 1];
+      kmag(w, kq);
+      float2 acc[E];
+#pragma unroll
+      for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
+      for (int b = 0; b < a.nb; ++b) {
+        float2 v[E];
+        gload(w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride, v);
+        PlanRun<P>::template run<false, true>(v, buf, t, tws, sync);
+        float wv[E];
+        wvals(kq, s_kr[b], wv);
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          acc[m].x = fmaf(wv[m], v[m].x, acc[m].x);
+          acc[m].y = fmaf(wv[m], v[m].y, acc[m].y);
+        }
+      }
+      float2* q = w.sg.out + w.off + (long long)t * w.sg.row_stride + c;
+      const long long step = (long long)G * w.sg.row_stride;
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        float2 o = a.first ? make_float2(0.f, 0.f) : q[m * step];
+        q[m * step] = make_float2(o.x + acc[m].x, o.y + acc[m].y);
+      }
+    }
+  }
+}
+
+}  // namespace prc

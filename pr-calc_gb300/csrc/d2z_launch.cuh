@@ -1,16 +1,52 @@
 // d2z_launch.cuh — host launchers for one grid size; included by inst_*.cu.
 #pragma once
 #include "d2z_adjoint.cuh"
+#include "d2z_cols.cuh"
 #include "d2z_dispatch.h"
 #include "d2z_kernels.cuh"
 
 namespace prc {
 
-template <int N> struct Launchers {
+// Column passes: k_col (one lane per column) where CCfg<N> has a plan, else
+// k_tile (shared-memory staged tiles).
+template <int N, bool COL = CCfg<N>::on> struct ColLaunch;
+
+template <int N> struct ColLaunch<N, false> {
   using TT = TK<N>;
-  using LL = LK<N>;
+  static constexpr int THREADS = TT::THREADS, T = TT::T;
   static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);    // one tile
   static constexpr size_t TS2 = (size_t)TT::smem2_f2 * sizeof(float2);  // two tiles (TM_WIN)
+  template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_tile<N, MODE>); }
+  static size_t bytes(int mode) { return mode == TM_WIN ? TS2 : TS; }
+  static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    switch (mode) {
+      case TM_FWD: k_tile<N, TM_FWD><<<grid, THREADS, TS, st>>>(a); break;
+      case TM_INV: k_tile<N, TM_INV><<<grid, THREADS, TS, st>>>(a); break;
+      case TM_WIN: k_tile<N, TM_WIN><<<grid, THREADS, TS2, st>>>(a); break;
+      default: k_tile<N, TM_ACC><<<grid, THREADS, TS, st>>>(a); break;
+    }
+  }
+};
+
+template <int N> struct ColLaunch<N, true> {
+  using CC = CK<N>;
+  static constexpr int THREADS = CC::THREADS, T = CC::T;
+  static constexpr size_t CS = (size_t)CC::smem_f2 * sizeof(float2);
+  template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_col<N, MODE>); }
+  static size_t bytes(int) { return CS; }
+  static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    switch (mode) {
+      case TM_FWD: k_col<N, TM_FWD><<<grid, THREADS, CS, st>>>(a); break;
+      case TM_INV: k_col<N, TM_INV><<<grid, THREADS, CS, st>>>(a); break;
+      case TM_WIN: k_col<N, TM_WIN><<<grid, THREADS, CS, st>>>(a); break;
+      default: k_col<N, TM_ACC><<<grid, THREADS, CS, st>>>(a); break;
+    }
+  }
+};
+
+template <int N> struct Launchers {
+  using CL = ColLaunch<N>;
+  using LL = LK<N>;
   static constexpr size_t LS = (size_t)LL::smem_f2 * sizeof(float2);
 
   template <class F> static cudaError_t smem(F fn, size_t bytes) {
@@ -22,22 +58,22 @@ template <int N> struct Launchers {
     return e;
   }
   static cudaError_t init(KernelSet* ks) {
-    void (*tf)(TileArgs) = &k_tile<N, TM_FWD>;
-    void (*ti)(TileArgs) = &k_tile<N, TM_INV>;
-    void (*tw)(TileArgs) = &k_tile<N, TM_WIN>;
-    void (*ta)(TileArgs) = &k_tile<N, TM_ACC>;
+    void* tf = CL::template fn<TM_FWD>();
+    void* ti = CL::template fn<TM_INV>();
+    void* tw = CL::template fn<TM_WIN>();
+    void* ta = CL::template fn<TM_ACC>();
     cudaError_t e;
-    if ((e = smem(tf, TS)) != cudaSuccess) return e;
-    if ((e = smem(ti, TS)) != cudaSuccess) return e;
-    if ((e = smem(tw, TS2)) != cudaSuccess) return e;
-    if ((e = smem(ta, TS)) != cudaSuccess) return e;
+    if ((e = smem(tf, CL::bytes(TM_FWD))) != cudaSuccess) return e;
+    if ((e = smem(ti, CL::bytes(TM_INV))) != cudaSuccess) return e;
+    if ((e = smem(tw, CL::bytes(TM_WIN))) != cudaSuccess) return e;
+    if ((e = smem(ta, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile, ti, TT::THREADS, TS)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile_win, tw, TT::THREADS, TS2)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile_acc, ta, TT::THREADS, TS)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile_win, tw, CL::THREADS, CL::bytes(TM_WIN))) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile_acc, ta, CL::THREADS, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r, &k_c2r_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_adj_z, &k_adj_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
@@ -48,12 +84,7 @@ template <int N> struct Launchers {
     k_r2c_z<N><<<grid, LL::THREADS, LS, st>>>(d, dinit, S, Qt, tw);
   }
   static void tile(const KernelSet&, int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
-    switch (mode) {
-      case TM_FWD: k_tile<N, TM_FWD><<<grid, TT::THREADS, TS, st>>>(a); break;
-      case TM_INV: k_tile<N, TM_INV><<<grid, TT::THREADS, TS, st>>>(a); break;
-      case TM_WIN: k_tile<N, TM_WIN><<<grid, TT::THREADS, TS2, st>>>(a); break;
-      default: k_tile<N, TM_ACC><<<grid, TT::THREADS, TS, st>>>(a); break;
-    }
+    CL::launch(mode, grid, st, a);
   }
   static void c2r_z(const KernelSet&, int grid, cudaStream_t st, const SweepArgs& a) {
     k_c2r_z<N><<<grid, LL::THREADS, LS, st>>>(a);
@@ -67,11 +98,11 @@ template <int N> struct Launchers {
   static KernelSet make() {
     KernelSet ks{};
     ks.N = N;
-    ks.tile_threads = TT::THREADS;
-    ks.tile_w = TT::T;
+    ks.tile_threads = CL::THREADS;
+    ks.tile_w = CL::T;
     ks.line_threads = LL::THREADS;
     ks.line_groups = LL::NG;
-    ks.tile_smem = TS;
+    ks.tile_smem = CL::bytes(TM_INV);
     ks.line_smem = LS;
     ks.init = &init;
     ks.r2c_z = &r2c_z;

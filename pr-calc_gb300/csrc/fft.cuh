@@ -227,17 +227,21 @@ template <int L, int TWS, int Ns, int OFF, int R, int... Rest> struct TwFill<L, 
 // Buf provides thread(tp) / get(h, cp) / put(h, cp, v) for split positions and
 // get_pos / put_pos for general ones; SPLIT (power-of-two G and radices)
 // selects the former.  tws: the stage twiddle tables, OFF this stage's offset.
-template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF, int... Rs> struct Stages;
+// PP (ping-pong): Buf holds two exchange buffers and flip() swaps them after
+// each exchange, so one barrier per exchange suffices (the next exchange
+// writes the other buffer, which every thread finished reading before the
+// barrier it has just passed).
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF, int... Rs> struct Stages;
 
-template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF> struct Stages<L, E, INV, SPLIT, Ns, OFF> {
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF> struct Stages<L, E, INV, SPLIT, PP, Ns, OFF> {
   template <class Buf, class Sync>
-  static __device__ __forceinline__ void run(float2 (&)[E], const Buf&, int, const float2*, const Sync&) {}
+  static __device__ __forceinline__ void run(float2 (&)[E], Buf&, int, const float2*, const Sync&) {}
 };
 
-template <int L, int E, bool INV, bool SPLIT, int Ns, int OFF, int R, int... Rest>
-struct Stages<L, E, INV, SPLIT, Ns, OFF, R, Rest...> {
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF, int R, int... Rest>
+struct Stages<L, E, INV, SPLIT, PP, Ns, OFF, R, Rest...> {
   template <class Buf, class Sync>
-  static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, int t, const float2* tws,
+  static __device__ __forceinline__ void run(float2 (&v)[E], Buf& buf, int t, const float2* tws,
                                              const Sync& sync) {
     constexpr int G = L / E;
     constexpr int Q = E / R;
@@ -284,8 +288,9 @@ struct Stages<L, E, INV, SPLIT, Ns, OFF, R, Rest...> {
 #pragma unroll
         for (int m = 0; m < E; ++m) v[m] = buf.get_pos(t + G * m);
       }
-      sync();
-      Stages<L, E, INV, SPLIT, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(v, buf, t, tws, sync);
+      if constexpr (PP) buf.flip();
+      else sync();
+      Stages<L, E, INV, SPLIT, PP, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(v, buf, t, tws, sync);
     }
   }
 };
@@ -301,10 +306,10 @@ template <int E, int... R> struct PlanRun<Plan<E, R...>> {
   static __device__ __forceinline__ void fill(float2* tws, const float2* tabN) {
     TwFill<L, TWS, 1, 0, R...>::run(tws, tabN);
   }
-  template <bool INV, class Buf, class Sync>
-  static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, int t, const float2* tws,
+  template <bool INV, bool PP = false, class Buf, class Sync>
+  static __device__ __forceinline__ void run(float2 (&v)[E], Buf& buf, int t, const float2* tws,
                                              const Sync& sync) {
-    Stages<L, E, INV, SPLIT, 1, 0, R...>::run(v, buf, t, tws, sync);
+    Stages<L, E, INV, SPLIT, PP, 1, 0, R...>::run(v, buf, t, tws, sync);
   }
 };
 
