@@ -352,7 +352,7 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig) {
     run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), nb);
     {
       Prof pf(c, PRC_KIND_C2R_Z);
-      c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, sa);
+      c->ks->c2r_z(c->ksl, grid_for(N * N, c->ksl.c2r_lines, c->ksl.occ_c2r, c->sms), c->st, sa);
     }
     c->launches++;
   }
@@ -580,7 +580,7 @@ int prc_d2z_smooth(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, 
   fa.tw = c->tw;
   fa.out = d_out;
   fa.scale = (float)(1.0 / (double)n3);
-  c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, fa);
+  c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r_plain, c->sms), c->st, fa);
   c->launches++;
   PRC_CU(cudaGetLastError(), "kernel launch");
   if (!out_on_device)
@@ -689,7 +689,7 @@ int prc_d2z_backward(prc_d2z_ctx* c, const float* dL_dz, const uint8_t* argmax, 
   fa.scale = (float)(1.0 / ((double)n3 * c->dinit));
   {
     Prof pf(c, PRC_KIND_C2R_PLAIN);
-    c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r, c->sms), c->st, fa);
+    c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r_plain, c->sms), c->st, fa);
   }
   c->launches++;
   PRC_CU(cudaGetLastError(), "kernel launch");

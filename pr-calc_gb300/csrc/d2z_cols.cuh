@@ -132,9 +132,25 @@ __global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a)
   // W(|k| R_b) of all E rows: rows m > E/2 mirror rows of the partner lane
   // (G - t, register E-1-m) or, in warp 0, of this lane (t = 0: E-m; t = G/2:
   // E-1-m)
+  // (the Taylor branch runs only in warps where some lane needs it)
   auto wvals = [&](const float (&kq)[EH + 1], float kr, float (&wv)[E]) {
+    bool small = false;
 #pragma unroll
-    for (int m = 0; m <= EH; ++m) wv[m] = (kq[m] < 0.f) ? 0.f : tophat(kq[m] * kr);
+    for (int m = 0; m <= EH; ++m) {
+      const float x = kq[m] * kr;
+      wv[m] = tophat_big(x);
+      small |= (x < 1.0f);
+    }
+    if (__any_sync(0xffffffffu, small)) {
+#pragma unroll
+      for (int m = 0; m <= EH; ++m) {
+        const float x = kq[m] * kr;
+        if (x < 1.0f) wv[m] = tophat_small(x);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m <= EH; ++m)
+      if (kq[m] < 0.f) wv[m] = 0.f;
 #pragma unroll
     for (int m = EH + 1; m < E; ++m) {
       const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);

@@ -14,9 +14,10 @@ struct KernelSet {
   int N;
   int tile_threads, tile_w;     // threads per column-pass CTA, columns per tile
   int line_threads, line_groups;  // threads per line-pass CTA, lines per CTA step
+  int c2r_lines;                  // lines per CTA step of the inverse z pass
   size_t tile_smem, line_smem;  // dynamic shared memory bytes
   // resident CTAs per SM (filled by init)
-  int occ_tile, occ_tile_win, occ_tile_acc, occ_r2c, occ_c2r, occ_adj_z;
+  int occ_tile, occ_tile_win, occ_tile_acc, occ_r2c, occ_c2r, occ_c2r_plain, occ_adj_z;
   cudaError_t (*init)(KernelSet*);
   void (*r2c_z)(const KernelSet&, int grid, cudaStream_t, const float* delta, float dinit,
                 float2* S, float2* Qt, const float2* tw);

@@ -138,29 +138,36 @@ __device__ __forceinline__ int fsq(int f, int n) {
 }
 
 // Top-hat window W(x) = 3 (sin x - x cos x) / x^3 (delta2zreion_d2z.C:77).
-// x < 1: the Taylor series sum_m 3 (-1)^m (2m+2) x^{2m} / (2m+3)! (no
-// cancellation).  x >= 1: Cody-Waite reduction of x by 2 pi = C1 + C2 (C1 the
-// float nearest 2 pi; the first FMA is exact for x < 2^10 * 2 pi) to [-pi, pi],
-// then the SFU sine/cosine (absolute error < 2^-21 there).
-__device__ __forceinline__ float tophat(float x) {
-  if (x < 1.0f) {
-    const float x2 = x * x;
-    float p = 3.2118087673643226e-11f;
-    p = fmaf(p, x2, -5.7812557812557812e-09f);
-    p = fmaf(p, x2, 7.5156325156325156e-07f);
-    p = fmaf(p, x2, -6.6137566137566138e-05f);
-    p = fmaf(p, x2, 3.5714285714285714e-03f);
-    p = fmaf(p, x2, -0.1f);
-    p = fmaf(p, x2, 1.0f);
-    return p;
-  }
+// x < 1 (tophat_small): the Taylor series sum_m 3 (-1)^m (2m+2) x^{2m} /
+// (2m+3)! (no cancellation).  x >= 1 (tophat_big): Cody-Waite reduction of x
+// by 2 pi = C1 + C2 (C1 the float nearest 2 pi; the first FMA is exact for
+// x < 2^10 * 2 pi) to [-pi, pi], then the SFU sine/cosine (absolute error
+// < 2^-21 there) and the SFU reciprocal (relative error ~2^-23).
+__device__ __forceinline__ float tophat_small(float x) {
+  const float x2 = x * x;
+  float p = 3.2118087673643226e-11f;
+  p = fmaf(p, x2, -5.7812557812557812e-09f);
+  p = fmaf(p, x2, 7.5156325156325156e-07f);
+  p = fmaf(p, x2, -6.6137566137566138e-05f);
+  p = fmaf(p, x2, 3.5714285714285714e-03f);
+  p = fmaf(p, x2, -0.1f);
+  p = fmaf(p, x2, 1.0f);
+  return p;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float tophat_big(float x) {
   const float k = rintf(x * 0.159154943091895336f);
   float r = fmaf(-k, 6.28318548202514648f, x);
   r = fmaf(-k, -1.74845560e-07f, r);
   const float s = __sinf(r), c = __cosf(r);
-  const float ix = __frcp_rn(x);
+  const float ix = rcp_approx(x);
   return 3.0f * fmaf(-x, c, s) * (ix * ix * ix);
 }
+__device__ __forceinline__ float tophat(float x) { return x < 1.0f ? tophat_small(x) : tophat_big(x); }
 
 __device__ __forceinline__ float window_of(int m2, float kr) {
   return (m2 == 0) ? 0.f : tophat(sqrtf((float)m2) * kr);

@@ -4,6 +4,7 @@
 #include "d2z_cols.cuh"
 #include "d2z_dispatch.h"
 #include "d2z_kernels.cuh"
+#include "d2z_lines.cuh"
 
 namespace prc {
 
@@ -44,8 +45,29 @@ template <int N> struct ColLaunch<N, true> {
   }
 };
 
+// Inverse z pass: k_c2r_zp (mirror pairs in one lane) where PCfg<N> has a
+// plan, else k_c2r_z.
+template <int N, bool PAIR = PCfg<N>::on> struct C2rLaunch {
+  static constexpr int THREADS = LK<N>::THREADS, NG = LK<N>::NG;
+  static constexpr size_t BYTES = (size_t)LK<N>::smem_f2 * sizeof(float2);
+  static void* fn(bool = true) { return reinterpret_cast<void*>(&k_c2r_z<N>); }
+  static void launch(int grid, cudaStream_t st, const SweepArgs& a) { k_c2r_z<N><<<grid, THREADS, BYTES, st>>>(a); }
+};
+template <int N> struct C2rLaunch<N, true> {
+  static constexpr int THREADS = PK<N>::THREADS, NG = PK<N>::NG;
+  static constexpr size_t BYTES = (size_t)PK<N>::smem_f2 * sizeof(float2);
+  static void* fn(bool am = true) {
+    return am ? reinterpret_cast<void*>(&k_c2r_zp<N, true>) : reinterpret_cast<void*>(&k_c2r_zp<N, false>);
+  }
+  static void launch(int grid, cudaStream_t st, const SweepArgs& a) {
+    if (a.argmax) k_c2r_zp<N, true><<<grid, THREADS, BYTES, st>>>(a);
+    else k_c2r_zp<N, false><<<grid, THREADS, BYTES, st>>>(a);
+  }
+};
+
 template <int N> struct Launchers {
   using CL = ColLaunch<N>;
+  using CR = C2rLaunch<N>;
   using LL = LK<N>;
   static constexpr size_t LS = (size_t)LL::smem_f2 * sizeof(float2);
 
@@ -68,14 +90,16 @@ template <int N> struct Launchers {
     if ((e = smem(tw, CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = smem(ta, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
-    if ((e = smem(&k_c2r_z<N>, LS)) != cudaSuccess) return e;
+    if ((e = smem(CR::fn(true), CR::BYTES)) != cudaSuccess) return e;
+    if ((e = smem(CR::fn(false), CR::BYTES)) != cudaSuccess) return e;
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_win, tw, CL::THREADS, CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_acc, ta, CL::THREADS, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_c2r, &k_c2r_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_c2r, CR::fn(), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_c2r_plain, &k_c2r_plain<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_adj_z, &k_adj_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     return cudaSuccess;
   }
@@ -86,9 +110,7 @@ template <int N> struct Launchers {
   static void tile(const KernelSet&, int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     CL::launch(mode, grid, st, a);
   }
-  static void c2r_z(const KernelSet&, int grid, cudaStream_t st, const SweepArgs& a) {
-    k_c2r_z<N><<<grid, LL::THREADS, LS, st>>>(a);
-  }
+  static void c2r_z(const KernelSet&, int grid, cudaStream_t st, const SweepArgs& a) { CR::launch(grid, st, a); }
   static void adj_z(const KernelSet&, int grid, cudaStream_t st, const AdjArgs& a) {
     k_adj_z<N><<<grid, LL::THREADS, LS, st>>>(a);
   }
@@ -102,6 +124,7 @@ template <int N> struct Launchers {
     ks.tile_w = CL::T;
     ks.line_threads = LL::THREADS;
     ks.line_groups = LL::NG;
+    ks.c2r_lines = CR::NG;
     ks.tile_smem = CL::bytes(TM_INV);
     ks.line_smem = LS;
     ks.init = &init;

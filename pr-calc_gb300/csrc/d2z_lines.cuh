@@ -1,0 +1,217 @@
+// d2z_lines.cuh — the inverse z pass with mirror pairs held by one lane.
+//
+// The half-complex-to-real transform of a z line needs, for every k, both
+// X[k] and X[H-k].  Here lane t of a group of G = H/E lanes loads the pairs
+// (X[k], X[H-k]) for k = t + G*m, m < E/2, straight from the slot, computes
+// both packed values Z[k] and Z[H-k] from the one pair, keeps Z[k] and hands
+// Z[H-k] to lane G-t (which owns position H-k) with one shuffle.  The packed
+// sequence then goes through the half-length inverse complex FFT (E = 16: one
+// shared-memory exchange for H = 256), so the only shared-memory traffic of
+// the kernel is that exchange.
+//
+// Packing (FFTW c2r semantics, imaginary parts of X[0] and X[H] ignored):
+//   xe = X[k] + conj X[H-k],  xo = (X[k] - conj X[H-k]) e^{+2 pi i k/N},
+//   Z[k] = xe + i xo,  Z[H-k] = conj(xe) + i conj(xo)
+// (the second because e^{+2 pi i (H-k)/N} = -conj e^{+2 pi i k/N}); the
+// inverse FFT of Z gives (x[2p], x[2p+1]) at p.  Lane 0 pairs k = G*m with
+// G*(E-m): its k = 0 partner is X[H] (the Nyquist plane), its k = H/2 value is
+// its own mirror, and its received values sit one register low, which a
+// final shift corrects.
+//
+// Then, per radius of the sweep, the barrier crossing of delta2zreion_d2z.C
+// :206-216 (z = A/N^3 x + (A B_b - 1)) and the running max of :105-146 with
+// strict >, in registers; one zreion / argmax read-modify-write per sweep.
+#pragma once
+#include "d2z_kernels.cuh"
+
+namespace prc {
+
+template <int N> struct PCfg { static constexpr bool on = false; };
+template <> struct PCfg<32> { static constexpr bool on = true; using P = Plan<8, 8, 2>; };
+template <> struct PCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
+template <> struct PCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 3>; };
+template <> struct PCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
+template <> struct PCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct PCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
+template <> struct PCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
+template <> struct PCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; };
+
+template <int N> struct PK {
+  using P = typename PCfg<N>::P;
+  static constexpr int H = N / 2, E = P::E, G = H / E;
+  static_assert(PlanRun<P>::L == H, "line plan length");
+  static_assert(E % 2 == 0 && G >= 2 && G <= 32 && 32 % G == 0, "paired line shape");
+  static constexpr int THREADS = 256;
+  static constexpr int NG = THREADS / G;                // lines per CTA step
+  static constexpr int MINB = 2;
+  static constexpr int gsize = GroupBuf<H, G>::size;
+  static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;
+  static constexpr int STG = NG * H;                    // one staged step: NG whole lines (float2)
+  static_assert((STG * 8) % (16 * THREADS) == 0, "16-byte copies per thread");
+  // N-table, stage twiddles, group buffers, two staged steps, two Nyquist rows
+  static constexpr int smem_f2 = N + TW + NG * gsize + 2 * STG + 2 * NG;
+};
+
+// 16-byte asynchronous global -> shared copy (L2 only).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// Steps (line group s, radius b) run in order; the input of the next step is
+// copied into the other staging buffer with cp.async while the current one is
+// transformed (the NG lines of a step are one contiguous block of the slot).
+// AM: argmax wanted (a.argmax != null); its bytes are packed four to a register.
+template <int N, bool AM>
+__global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArgs a) {
+  using KK = PK<N>;
+  using P = typename KK::P;
+  constexpr int H = N / 2, E = KK::E, G = KK::G, NG = KK::NG, EH = E / 2, STG = KK::STG;
+  constexpr long long NN = (long long)N * N;
+  static_assert((NN % NG) == 0, "whole line groups");
+  extern __shared__ float4 smem4[];
+  float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* tws = tw + N;
+  float2* gb = tws + KK::TW;
+  float2* stage = gb + NG * KK::gsize;  // 16-byte aligned: N, TW, gsize are even
+  float2* nyq = stage + 2 * STG;
+  load_tw(tw, a.tw, N);
+  PlanRun<P>::template fill<2>(tws, a.tw);
+  __shared__ double red[kMaxBatch];
+  __shared__ float s_cb[kMaxBatch];
+  stage_params(s_cb, a.cb);
+  if (threadIdx.x < kMaxBatch) red[threadIdx.x] = 0.0;
+  const int g = threadIdx.x / G, t = threadIdx.x % G;
+  const LineBuf<H> buf{gb + g * KK::gsize};
+  GroupSync<G> sync(g);
+  const int partner = (G - t) & (G - 1);
+  const bool want_sig = a.sig_acc != nullptr;
+  const int nsteps_l = (int)((NN / NG - blockIdx.x + gridDim.x - 1) / gridDim.x);  // line groups of this CTA
+  const int nb = a.nb;
+  const int total = nsteps_l > 0 ? nsteps_l * nb : 0;
+
+  // copies of step i = (line group i / nb, radius i % nb) into staging buffer i & 1
+  auto issue = [&](int i) {
+    if (i < total) {
+      const long long l0 = ((long long)blockIdx.x + (long long)(i / nb) * gridDim.x) * NG;
+      const int b = i % nb;
+      const float2* slot = a.slots + (long long)b * a.slot_stride;
+      const char* src = reinterpret_cast<const char*>(slot + l0 * H);
+      char* dst = reinterpret_cast<char*>(stage + (i & 1) * STG);
+#pragma unroll
+      for (int q = 0; q < (STG * 8) / (16 * KK::THREADS); ++q) {
+        const int off = (q * KK::THREADS + threadIdx.x) * 16;
+        cp_async16(dst + off, src + off);
+      }
+      if (t == 0) {
+        const long long l = l0 + g;
+        const int ix = (int)(l / N), iy = (int)(l - (l / N) * N);
+        cp_async8(nyq + (i & 1) * NG + g, slot + NN * H + (long long)iy * N + ix);
+      }
+    }
+    cp_async_commit();
+  };
+
+  issue(0);
+  float2 zr[E];
+  uint32_t am[AM ? EH : 1];  // argmax bytes of cells 2p, 2p+1 of elements 2j (low half) and 2j+1
+  for (int i = 0; i < total; ++i) {
+    const int b = i % nb;
+    const long long l = ((long long)blockIdx.x + (long long)(i / nb) * gridDim.x) * NG + g;
+    float* zline = a.zreion + l * N;
+    uint16_t* aline = AM ? reinterpret_cast<uint16_t*>(a.argmax + l * N) : nullptr;
+    if (b == 0) {
+      if (a.first) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) zr[m] = make_float2(0.f, 0.f);
+        if constexpr (AM) {
+#pragma unroll
+          for (int j = 0; j < EH; ++j) am[j] = 0xFFFFFFFFu;
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; ++m) zr[m] = reinterpret_cast<const float2*>(zline)[t + G * m];
+        if constexpr (AM) {
+#pragma unroll
+          for (int j = 0; j < EH; ++j)
+            am[j] = (uint32_t)aline[t + G * (2 * j)] | ((uint32_t)aline[t + G * (2 * j + 1)] << 16);
+        }
+      }
+    }
+    cp_async_wait<0>();
+    __syncthreads();  // step i staged for everyone; everyone is done reading buffer (i+1) & 1
+    issue(i + 1);
+    const float2* src = stage + (i & 1) * STG + g * H;
+    float2 v[E];
+    float2 mir[EH];
+#pragma unroll
+    for (int m = 0; m < EH; ++m) {
+      float2 x = src[t + G * m];
+      float2 xp = (m == 0 && t == 0) ? nyq[(i & 1) * NG + g] : src[H - t - G * m];
+      if (m == 0 && t == 0) {
+        x.y = 0.f;
+        xp.y = 0.f;
+      }
+      const float2 xc = cconj(xp);
+      const float2 xe = cadd(x, xc);
+      const float2 xo = cmul(csub(x, xc), tw[t + G * m]);
+      v[m] = make_float2(xe.x - xo.y, xe.y + xo.x);
+      mir[m] = make_float2(xe.x + xo.y, xo.x - xe.y);
+    }
+    const float2 xm = src[H / 2];
+    // Z[H-k] to the lane that owns it (lane G-t, register E-1-m)
+#pragma unroll
+    for (int m = 0; m < EH; ++m) {
+      v[E - 1 - m].x = __shfl_sync(0xffffffffu, mir[m].x, partner, G);
+      v[E - 1 - m].y = __shfl_sync(0xffffffffu, mir[m].y, partner, G);
+    }
+    if (t == 0) {
+      // lane 0 received its own mirrors Z[G*(E-m)] one register low
+#pragma unroll
+      for (int j = E - 1; j > EH; --j) v[j] = v[j - 1];
+      const float2 xc = cconj(xm);
+      const float2 xe = cadd(xm, xc);
+      const float2 xo = cmul(csub(xm, xc), tw[H / 2]);
+      v[EH] = make_float2(xe.x - xo.y, xe.y + xo.x);
+    }
+    PlanRun<P>::template run<true>(v, buf, t, tws, sync);
+    const float cb = s_cb[b];
+    const uint32_t rid = (uint32_t)(a.r0 + b);
+    float ss = 0.f;
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const float x0 = v[m].x, x1 = v[m].y;
+      const float z0 = fmaf(a.as, x0, cb), z1 = fmaf(a.as, x1, cb);
+      const int sh = 16 * (m & 1);
+      if (z0 > zr[m].x) {
+        zr[m].x = z0;
+        if constexpr (AM) am[m >> 1] = (am[m >> 1] & ~(0xFFu << sh)) | (rid << sh);
+      }
+      if (z1 > zr[m].y) {
+        zr[m].y = z1;
+        if constexpr (AM) am[m >> 1] = (am[m >> 1] & ~(0xFF00u << sh)) | (rid << (sh + 8));
+      }
+      ss = fmaf(x0, x0, fmaf(x1, x1, ss));
+    }
+    if (want_sig) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+      if ((threadIdx.x & 31) == 0) atomicAdd(&red[b], (double)ss);
+    }
+    if (b == nb - 1) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const int p = t + G * m;
+        reinterpret_cast<float2*>(zline)[p] = zr[m];
+        if constexpr (AM) aline[p] = (uint16_t)(am[m >> 1] >> (16 * (m & 1)));
+      }
+    }
+  }
+  cp_async_wait<0>();
+  if (want_sig) {
+    __syncthreads();
+    if (threadIdx.x < a.nb) atomicAdd(&a.sig_acc[a.r0 + threadIdx.x], red[threadIdx.x]);
+  }
+}
+
+}  // namespace prc

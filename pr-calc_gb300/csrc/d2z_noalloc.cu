@@ -193,7 +193,7 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     sa.first = (r == 0);
     sa.as = (float)(barrier_a / n3);
     sa.cb[0] = (float)(barrier_a * barrier_b[r] - 1.0);
-    ks.c2r_z(ks, grid_of((N * N + ks.line_groups - 1) / ks.line_groups, ks.occ_c2r, sms), st, sa);
+    ks.c2r_z(ks, grid_of((N * N + ks.c2r_lines - 1) / ks.c2r_lines, ks.occ_c2r, sms), st, sa);
   }
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
