@@ -44,6 +44,15 @@ MMIN_MSUN = 1e9 / H_
 ZETA = 80.5404       # 512^3, 600 Mpc/h, 64 radii to 60 Mpc/h
 ZETA_BATCH = 81.6855 # 256^3, 384 Mpc/h (1.5 Mpc/h cells), 48 radii to 60 Mpc/h
 CPU_SAMPLE_RADII = 4
+# plain configurations: N, box [Mpc/h], radii, calibrated zeta (x_i(z=8) = 0.5 at seed 1)
+CONFIGS = {"C1": (128, 200.0, 32, 82.4429), "C2": (512, 600.0, 64, 80.5404), "C3": (1024, 1200.0, 96, 73.1587)}
+
+
+def _use_config(name):
+    """Select a plain configuration (C2, 512^3 x 64, is the default workload)."""
+    global N_DEF, BOX, NR, ZETA, METRIC
+    N_DEF, BOX, NR, ZETA = CONFIGS[name]
+    METRIC = f"zreion cell*radii/s at {N_DEF}^3 ({NR} radii)"
 
 
 def _peaks():
@@ -205,6 +214,7 @@ def run_ours(args, rank, world, local_rank):
 
     import prc_d2z
     from prc_d2z import fields
+    from prc_d2z.parallel import max_over_ranks
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
     N = args.n
@@ -236,10 +246,7 @@ def run_ours(args, rank, world, local_rank):
     prof = ctx.profile_read()
     ctx.profile(False)
     launches = ctx.last_launches() * args.steps
-    if world > 1:
-        tt = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(tt.item())
+    ms_total = max_over_ranks(ms_total, device=dev)
     ms_step = ms_total / args.steps
     value = world * N ** 3 * NR / (ms_step * 1e-3)
 
@@ -257,10 +264,7 @@ def run_ours(args, rank, world, local_rank):
         ctx.forward(hd, zreion=hz, want_argmax=False)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(e2e_s, device=dev)
     e2e = world * N ** 3 * NR * args.steps / e2e_s
 
     if rank != 0:
@@ -443,13 +447,17 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEF)
+    ap.add_argument("--config", default="C2", choices=sorted(CONFIGS))
+    ap.add_argument("--n", type=int, default=0, help="grid side (default: the config's; keeps its cell size)")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--ref-radii", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
     ap.add_argument("--streams", type=int, default=4)
     args = ap.parse_args()
+    _use_config(args.config)
+    if args.n == 0:
+        args.n = N_DEF
     if args.workload == "batched" and args.impl == "ours":
         run_batched(args)
         return

@@ -105,6 +105,16 @@ typedef struct {
   void*         stream;           /* cudaStream_t; NULL = default stream        */
 } prc_d2z_desc;
 
+/* Synthetic input fields (the producer of delta_lin; the role of the ics
+ * generator, grf_ics.C:8-112, whose drand48 + Marsaglia-polar stream is
+ * sequential by construction and is replaced by a counter-based one).
+ *
+ * prc_white_noise: n unit Gaussians into device memory, cell i from
+ * Philox4x32-10 with counter (i mod 2^32, i div 2^32, 0, 0) and key (seed, 0),
+ * Box-Muller in FP64 on words 0 and 1, rounded to float32; stream-ordered,
+ * no synchronisation.  No counterpart in the reference. */
+int prc_white_noise(float* d_out, long long n, unsigned int seed, void* stream);
+
 /* Replaces the barrier table of a context (same radii): B_r and A as in the
  * descriptor.  For parameter scans (e.g. zeta) without a new workspace. */
 int prc_d2z_set_barrier(prc_d2z_ctx* ctx, const double* barrier_b, double barrier_a);
@@ -131,6 +141,16 @@ int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_devic
  * prc_d2z_forward, which never materialises delta_R. */
 int prc_d2z_smooth(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_device, int radius,
                    float* delta_r, int out_on_device);
+
+/* A Gaussian random field on the context's grid, written to delta (N^3 float32,
+ * file order): w = prc_white_noise(seed), then delta = C2R(amp[|m|^2] * R2C(w)),
+ * |m|^2 = fx^2 + fy^2 + fz^2 over the folded integer wavenumbers (|f| <= N/2).
+ * amp (host, n_amp >= 3*(N/2)^2 + 1 floats) carries the whole spectral shape
+ * and normalisation, including the 1/N^3 of the inverse transform and
+ * amp[0] = 0; e.g. sqrt(N^3 P(k)/L^3)/N^3 gives the normalisation of
+ * grf_ics.C:20-28,49-78.  Uses the context's spectrum and first radius slot. */
+int prc_d2z_gaussian_field(prc_d2z_ctx* ctx, unsigned int seed, const float* amp, int n_amp,
+                           float* delta, int out_on_device);
 
 /* Ionisation-history histogram of a zreion grid (bubblehistory_d2z.C:17-34):
  * counts[PRC_NHISTORY] raw bin counts (optional) and history[PRC_NHISTORY], the

@@ -123,6 +123,62 @@ __global__ void k_remap(float* __restrict__ z, long long n, const float* __restr
   }
 }
 
+// ---------------------------------------------------------------- field generator
+// Unit Gaussian white noise per cell: Philox4x32-10 (Salmon et al., SC 2011)
+// with counter (cell & 0xffffffff, cell >> 32, 0, 0) and key (seed, 0), then
+// Box-Muller in FP64 on words 0 and 1: sqrt(-2 ln u1) cos(2 pi u2),
+// u = (word + 1/2) / 2^32.  Rounded to float32.
+__global__ void k_white_noise(float* __restrict__ out, long long n, uint32_t seed) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t c0 = (uint32_t)(i & 0xffffffffll), c1 = (uint32_t)(i >> 32), c2 = 0u, c3 = 0u;
+    uint32_t k0 = seed, k1 = 0u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+      if (r) {
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+      }
+      const uint32_t hi0 = __umulhi(c0, 0xD2511F53u), lo0 = c0 * 0xD2511F53u;
+      const uint32_t hi1 = __umulhi(c2, 0xCD9E8D57u), lo1 = c2 * 0xCD9E8D57u;
+      const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+      c0 = n0;
+      c1 = lo1;
+      c2 = n2;
+      c3 = lo0;
+    }
+    const double u1 = ((double)c0 + 0.5) / 4294967296.0;
+    const double u2 = ((double)c1 + 0.5) / 4294967296.0;
+    out[i] = (float)(sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2));
+  }
+}
+
+// Half spectrum (main X[ix][iy][kz<H] and the Nyquist plane Q[ix][iy]) times
+// amp[|m|^2], |m|^2 = fx^2 + fy^2 + kz^2 with f folded to |f| <= N/2.
+__global__ void k_grf_amp(float2* __restrict__ spec, int N, const float* __restrict__ amp) {
+  const int H = N / 2;
+  const long long NN = (long long)N * N, total = NN * (H + 1);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    int ix, iy, kz;
+    if (i < NN * H) {
+      kz = (int)(i % H);
+      const long long l = i / H;
+      ix = (int)(l / N);
+      iy = (int)(l % N);
+    } else {
+      const long long q = i - NN * H;
+      ix = (int)(q / N);
+      iy = (int)(q % N);
+      kz = H;
+    }
+    const int fx = ix <= H ? ix : N - ix, fy = iy <= H ? iy : N - iy;
+    const float a = amp[fx * fx + fy * fy + kz * kz];
+    const float2 v = spec[i];
+    spec[i] = make_float2(v.x * a, v.y * a);
+  }
+}
+
 }  // namespace prc
 
 using namespace prc;
@@ -147,6 +203,7 @@ struct prc_d2z_ctx {
   uint32_t* counts = nullptr;
   float* gstage = nullptr;
   uint8_t* amstage = nullptr;
+  float* grf_amp = nullptr;       // field generator: amplitude by |m|^2
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float last_ms[3] = {0, 0, 0};
   int have_timing = 0;
@@ -234,6 +291,7 @@ void free_all(prc_d2z_ctx* c) {
   cudaFree(c->counts);
   cudaFree(c->gstage);
   cudaFree(c->amstage);
+  cudaFree(c->grf_amp);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->pev) cudaEventDestroy(e);
@@ -306,8 +364,8 @@ int set_device(prc_d2z_ctx* c) {
   return PRC_OK;
 }
 
-// R2C of delta_lin (device) into c->spec.
-void forward_r2c(prc_d2z_ctx* c, const float* d_delta) {
+// R2C of delta_lin / divisor (device) into c->spec.
+void forward_r2c(prc_d2z_ctx* c, const float* d_delta, double divisor) {
   const int N = c->N, H = c->H;
   const long long NN = c->NN;
   float2* S = c->spec;
@@ -316,7 +374,7 @@ void forward_r2c(prc_d2z_ctx* c, const float* d_delta) {
   {
     Prof pf(c, PRC_KIND_R2C_Z);
     c->ks->r2c_z(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_r2c, c->sms), c->st, d_delta,
-                 (float)c->dinit, S, Qt, c->tw);
+                 (float)divisor, S, Qt, c->tw);
   }
   c->launches++;
   // y pass: main in place; Nyquist Qt[iy][ix] -> Q[ix][ky]
@@ -392,7 +450,7 @@ void batch_enqueue(prc_d2z_batch* b, const float* const* delta, float* const* zr
   for (int i = 0; i < b->n; ++i) {
     prc_d2z_ctx* c = b->ctx[i];
     c->launches = 0;
-    forward_r2c(c, delta[i]);
+    forward_r2c(c, delta[i], c->dinit);
     enqueue_sweeps(c, zreion[i], argmax ? argmax[i] : nullptr, nullptr);
   }
   for (size_t k = 0; k < b->streams.size(); ++k) {
@@ -516,7 +574,7 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
   if (want_sig) PRC_CU(cudaMemsetAsync(c->sig, 0, sizeof(double) * c->nr, c->st), "memset sigma");
 
   PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
-  forward_r2c(c, d_delta);
+  forward_r2c(c, d_delta, c->dinit);
   PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
   enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr);
   PRC_CU(cudaGetLastError(), "kernel launch");
@@ -570,7 +628,7 @@ int prc_d2z_smooth(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, 
     if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "output stage")) != PRC_OK) return st;
     d_out = c->zre;
   }
-  forward_r2c(c, d_delta);
+  forward_r2c(c, d_delta, c->dinit);
   float2* U = c->slots;
   run_tile(c, TM_WIN, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1, 1, radius);
   run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), 1);
@@ -587,6 +645,64 @@ int prc_d2z_smooth(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, 
     PRC_CU(cudaMemcpyAsync(delta_r, d_out, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H delta_R");
   PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_smooth");
   prof_collect(c);
+  return PRC_OK;
+}
+
+int prc_white_noise(float* d_out, long long n, unsigned int seed, void* stream) {
+  if (!d_out || n < 0) return prc_fail(PRC_ERR_INVALID, "prc_white_noise: null output or negative count");
+  if (n == 0) return PRC_OK;
+  int dev = 0, sms = 0;
+  PRC_CU(cudaGetDevice(&dev), "cudaGetDevice");
+  PRC_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device query");
+  const long long need = (n + 255) / 256;
+  const int blocks = (int)(need < (long long)sms * 16 ? need : (long long)sms * 16);
+  k_white_noise<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_out, n, (uint32_t)seed);
+  PRC_CU(cudaGetLastError(), "k_white_noise launch");
+  return PRC_OK;
+}
+
+int prc_d2z_gaussian_field(prc_d2z_ctx* c, unsigned int seed, const float* amp, int n_amp, float* delta,
+                           int out_on_device) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (!amp || !delta) return prc_fail(PRC_ERR_INVALID, "prc_d2z_gaussian_field: null argument");
+  const int N = c->N, H = c->H;
+  const int need = 3 * H * H + 1;
+  if (n_amp < need)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_gaussian_field: amplitude table has %d entries, needs %d", n_amp, need);
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const long long NN = c->NN, n3 = NN * N;
+  c->launches = 0;
+  if (!c->grf_amp && (st = dalloc(&c->grf_amp, (size_t)need, "amplitude table")) != PRC_OK) return st;
+  PRC_CU(cudaMemcpyAsync(c->grf_amp, amp, sizeof(float) * need, cudaMemcpyHostToDevice, c->st), "H2D amplitudes");
+  float* d_out = delta;
+  if (!out_on_device) {
+    if (!c->zre && (st = dalloc(&c->zre, (size_t)n3, "output stage")) != PRC_OK) return st;
+    d_out = c->zre;
+  }
+  if ((st = prc_white_noise(d_out, n3, seed, c->st)) != PRC_OK) return st;
+  c->launches++;
+  forward_r2c(c, d_out, 1.0);
+  const long long total = NN * (H + 1);
+  const long long blk = (total + 255) / 256;
+  k_grf_amp<<<(int)(blk < (long long)c->sms * 16 ? blk : (long long)c->sms * 16), 256, 0, c->st>>>(c->spec, N,
+                                                                                                    c->grf_amp);
+  c->launches++;
+  float2* U = c->slots;
+  run_tile(c, TM_INV, mseg(c, c->spec, U, true), qseg(c, c->spec + NN * H, U + NN * H, true), 1);
+  run_tile(c, TM_INV, mseg(c, U, U, false), qseg(c, U + NN * H, U + NN * H, false), 1);
+  AdjArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  fa.slots = U;
+  fa.tw = c->tw;
+  fa.out = d_out;
+  fa.scale = 1.0f;
+  c->ks->c2r_plain(c->ksl, grid_for(N * N, c->ksl.line_groups, c->ksl.occ_c2r_plain, c->sms), c->st, fa);
+  c->launches++;
+  PRC_CU(cudaGetLastError(), "kernel launch");
+  if (!out_on_device)
+    PRC_CU(cudaMemcpyAsync(delta, d_out, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H field");
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_gaussian_field");
   return PRC_OK;
 }
 

@@ -464,6 +464,10 @@ __global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_A
       __syncthreads();
       float2 v[E];
       col_read(buf0, v);
+      // the column is also the exchange buffer: every lane of the group must
+      // have read it before the first stage writes it (a group of 64 lanes
+      // spans two warps)
+      sync();
       const TileCol<N> col{buf0, g};
       PlanRun<typename KK::P>::template run<INV>(v, col, t, tws, sync);
       col_write(buf0, v);
@@ -523,6 +527,7 @@ __global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_A
         __syncthreads();
         float2 v[E];
         col_read(tile, v);
+        sync();  // as above: the column is the exchange buffer
         float wv[E];
         window(w, b, wv);
         const TileCol<N> col{tile, g};

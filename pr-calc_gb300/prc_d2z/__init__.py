@@ -334,6 +334,21 @@ class Delta2Zreion:
                                _host_ptr(out, np.float32, self.n3), 0))
         return out
 
+    def gaussian_field(self, seed: int, amp, out=None):
+        """A Gaussian random field on this context's grid (prc_d2z_gaussian_field):
+        amp is the |m|^2-indexed amplitude table (fields.amplitude_table).  out:
+        a CUDA float32 tensor (N^3) or None for a host array."""
+        a = np.ascontiguousarray(amp, np.float32)
+        L = load()
+        if out is not None and _is_torch(out):
+            check(L.prc_d2z_gaussian_field(self._ctx, int(seed) & 0xFFFFFFFF, a.ctypes.data, len(a),
+                                           _dev_ptr(out.reshape(-1), "float32", self.n3), 1))
+            return out
+        res = np.empty((self.N,) * 3, np.float32) if out is None else out
+        check(L.prc_d2z_gaussian_field(self._ctx, int(seed) & 0xFFFFFFFF, a.ctypes.data, len(a),
+                                       _host_ptr(res, np.float32, self.n3), 0))
+        return res
+
     def set_barrier(self, barrier_b, barrier_a: float) -> None:
         """New barrier table for the same radii (prc_d2z_set_barrier)."""
         b = np.ascontiguousarray(barrier_b, np.float64)

@@ -83,6 +83,17 @@ def white_noise_torch(N: int, seed: int, device="cuda"):
     return out.reshape(N, N, N)
 
 
+def white_noise_native(N: int, seed: int, device="cuda"):
+    """white_noise() by this library's kernel (prc_white_noise), float32, on
+    the current CUDA stream of `device`."""
+    import torch
+    from . import _lib
+    out = torch.empty(N ** 3, dtype=torch.float32, device=device)
+    st = torch.cuda.current_stream(out.device).cuda_stream
+    _lib.check(_lib.load().prc_white_noise(out.data_ptr(), N ** 3, int(seed) & 0xFFFFFFFF, st))
+    return out.reshape(N, N, N)
+
+
 def bbks_transfer(k_hmpc, omegam: float, h: float):
     """T(q), q = k / Gamma with k in h/Mpc and Gamma = Omega_m h."""
     q = np.asarray(k_hmpc, np.float64) / (omegam * h)
@@ -122,9 +133,40 @@ def spectrum_amplitude(N: int, box_hmpc: float, omegam=0.31, h=0.68, ns=0.965, s
     return np.sqrt(N ** 3 * P / box_hmpc ** 3)
 
 
+def amplitude_table(N: int, box_hmpc: float, omegam=0.31, h=0.68, ns=0.965, sigma8=0.81) -> np.ndarray:
+    """sqrt(N^3 P(k) / L^3) / N^3 indexed by the integer |m|^2 = fx^2 + fy^2 + fz^2
+    (0 .. 3 (N/2)^2), k = (2 pi / L) sqrt(|m|^2): the table prc_d2z_gaussian_field
+    takes (the 1/N^3 is the inverse transform's normalisation)."""
+    amp = power_norm(omegam, h, ns, sigma8)
+    m2 = np.arange(3 * (N // 2) ** 2 + 1, dtype=np.float64)
+    k = (2 * math.pi / box_hmpc) * np.sqrt(m2)
+    with np.errstate(divide="ignore"):
+        P = np.where(k > 0, amp * k ** ns * bbks_transfer(k, omegam, h) ** 2, 0.0)
+    return (np.sqrt(N ** 3 * P / box_hmpc ** 3) / N ** 3).astype(np.float32)
+
+
 def gaussian_field(N: int, box_hmpc: float, seed: int = 1, omegam=0.31, h=0.68, ns=0.965, sigma8=0.81,
-                   backend: str = "numpy", device="cuda"):
-    """float32 delta_lin (N, N, N) at z = 0 in file order."""
+                   backend: str = "numpy", device="cuda", engine=None):
+    """float32 delta_lin (N, N, N) at z = 0 in file order.
+
+    backend "numpy" (host, FP64 transforms), "torch" (the same on a CUDA device
+    through torch.fft) or "native" (this library's kernels: Philox noise, the
+    float32 R2C / C2R passes of the step; `engine` is an optional
+    Delta2Zreion context of this N to use, else one is made)."""
+    if backend == "native":
+        import torch
+        from . import Delta2Zreion
+        tab = amplitude_table(N, box_hmpc, omegam, h, ns, sigma8)
+        own = engine is None
+        if own:
+            engine = Delta2Zreion(N, box_hmpc / h, [1.0], [0.0], 1.0, 1.0)
+        try:
+            out = torch.empty((N, N, N), dtype=torch.float32, device=device)
+            engine.gaussian_field(seed, tab, out=out)
+            return out
+        finally:
+            if own:
+                engine.close()
     S = spectrum_amplitude(N, box_hmpc, omegam, h, ns, sigma8)
     if backend == "torch":
         import torch

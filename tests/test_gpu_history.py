@@ -72,6 +72,10 @@ def test_executable_end_to_end(tmp_path):
     assert "Nscales" in used and "Bogus" not in used
     out = tmp_path / "output"
     zfile = np.fromfile(out / "run.zreion", np.float32).reshape(N, N, N)
+    # the consumers' slab reader (ReadReionFile at two ranks) sees the same field
+    from prc_d2z import io as pio
+    slabs = [pio.read_reion_file(str(out / "run.zreion"), N, 2, q)[0] for q in range(2)]
+    assert np.array_equal(np.concatenate(slabs), zfile)
     # the same chain through the Python API
     p = prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box)
     cl = prc_d2z.CLParameters(Rmax=20.0, zeta=30.0, M_min=1.47e9)
@@ -83,3 +87,19 @@ def test_executable_end_to_end(tmp_path):
     hist = np.loadtxt(out / "run.history")
     assert hist.shape == (100000, 4)
     assert (out / "run.mfp").exists() and (out / "run.mfppdf").stat().st_size == 8 + 16 + 4 * 200 * 1000
+
+
+def test_executable_requires_fcoll_table(tmp_path):
+    """Without fcoll_table.tab the history correction cannot run: the
+    executable stops with a message and writes no .zreion."""
+    exe = os.path.join(REPO, "pr-calc_gb300", "bin", "delta2zreion")
+    N, box = 16, 24.0
+    fields.gaussian_field(N, box, seed=7).tofile(tmp_path / "delta")
+    (tmp_path / "param.d2z").write_text(
+        "Omegam 0.31\nOmegal 0.69\nOmegab 0.049\nh 0.68\nns 0.965\nsigma8 0.81\nw -1\n"
+        f"BoxSize {box}\nN {N}\nzInit 0\nDeltaFile delta\nRmin 2\nNscales 4\n")
+    r = subprocess.run([exe, "param.d2z", "-f", "run", "-r", "9", "-v", "-e"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0
+    assert "fcoll_table.tab" in r.stdout
+    assert not (tmp_path / "output" / "run.zreion").exists()

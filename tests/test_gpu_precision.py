@@ -1,0 +1,107 @@
+"""Full-size precision runs: the GPU path at 512^3 x 64 radii (600 Mpc/h) and
+1024^3 x 96 radii (1200 Mpc/h) against an FP64 restatement of the whole chain
+computed with torch on the GPU (cuFFT in double precision; test-only).
+
+Tolerances: delta_R within 1e-5 relative RMS of FP64 for the first, a middle
+and the last radius; zreion within eps_z = A 1e-5 max|delta_R| + 2 ulp and the
+same argmax for every cell whose top-two margin (best vs runner-up radius, or
+vs the initial zreion = 0) exceeds eps_z; the near-barrier fraction is
+reported (about 1% at 512^3 x 64: adjacent radii of a dense log grid give
+close z) and must stay below 5%."""
+import math
+
+import numpy as np
+import pytest
+
+import prc_d2z
+from prc_d2z import fields
+
+pytestmark = pytest.mark.gpu
+H_ = 0.68
+
+
+def _kmag(N, box_mpc, device):
+    import torch
+    f = torch.fft.fftfreq(N, d=1.0 / N, device=device, dtype=torch.float64)
+    fz = torch.arange(N // 2 + 1, device=device, dtype=torch.float64)
+    dk = 2.0 * math.pi / box_mpc
+    k2 = (f[:, None, None] ** 2 + f[None, :, None] ** 2 + fz[None, None, :] ** 2) * dk * dk
+    return torch.sqrt(k2)
+
+
+def _tophat64(x):
+    import torch
+    small = x < 1e-2
+    xs = torch.where(small, torch.ones_like(x), x)
+    w = 3.0 * (torch.sin(xs) - xs * torch.cos(xs)) / xs ** 3
+    x2 = x * x
+    ws = 1.0 - x2 / 10.0 + x2 * x2 / 280.0
+    return torch.where(small, ws, w)
+
+
+def _fp64_chain(delta, box_mpc, R, A, B, dinit, radii_check):
+    """zreion / argmax / top-two margin / max|delta_R| and delta_R of the
+    radii in radii_check, all in FP64 on the GPU."""
+    import torch
+    N = delta.shape[0]
+    dev = delta.device
+    spec = torch.fft.rfftn(delta.double() / dinit)
+    kmag = _kmag(N, box_mpc, dev)
+    best = torch.full(delta.shape, -math.inf, dtype=torch.float64, device=dev)
+    second = best.clone()
+    am = torch.full(delta.shape, 255, dtype=torch.uint8, device=dev)
+    dmax = 0.0
+    keep = {}
+    for r in range(len(R)):
+        W = _tophat64(kmag * R[r])
+        W[0, 0, 0] = 0.0
+        dR = torch.fft.irfftn(spec * W, s=(N, N, N))
+        del W
+        dmax = max(dmax, float(dR.abs().max()))
+        if r in radii_check:
+            keep[r] = dR.clone()
+        z = A * (dR + B[r]) - 1.0
+        del dR
+        gt = z > best
+        second = torch.where(gt, best, torch.where(z > second, z, second))
+        best = torch.where(gt, z, best)
+        am[gt] = r
+        del z, gt
+    zo = torch.where(best > 0, best, torch.zeros_like(best))
+    am = torch.where(best > 0, am, torch.full_like(am, 255))
+    gap = torch.minimum(best - second, best.abs())
+    return zo, am, gap, dmax, keep
+
+
+@pytest.mark.parametrize("N,box,nr,zeta", [(512, 600.0, 64, 80.5404), (1024, 1200.0, 96, 73.1587)])
+def test_full_size_against_fp64(N, box, nr, zeta):
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    if free < (12 if N == 512 else 100) * 2 ** 30:
+        pytest.skip("not enough device memory for the FP64 restatement")
+    p = prc_d2z.Parameters(N=N, Nscales=nr, BoxSize=box, Rmin=2.0)
+    cl = prc_d2z.CLParameters(Rmax=60.0, zeta=zeta, M_min=1e9 / H_)
+    delta = fields.gaussian_field(N, box, seed=1, backend="torch").contiguous()
+    check = (0, nr // 2, nr - 1)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl) as ctx:
+        t = ctx.tables
+        box_mpc = float(np.float32(box) / np.float32(H_))
+        z, am, _ = ctx.forward(delta)
+        dRs = {r: ctx.smooth(delta, r) for r in check}
+        torch.cuda.synchronize()
+        zo, amo, gap, dmax, keep = _fp64_chain(delta, box_mpc, t.radii_mpc, t.barrier_a, t.barrier_b, t.DInit,
+                                               check)
+        for r in check:
+            d = dRs[r].double() - keep[r]
+            rel = math.sqrt(float((d * d).mean()) / float((keep[r] * keep[r]).mean()))
+            assert rel < 1e-5, (r, rel)
+        del keep, dRs
+        eps = t.barrier_a * 1e-5 * dmax + 2 * torch.abs(zo).float().nextafter(
+            torch.tensor(math.inf, device=zo.device)).sub(torch.abs(zo).float()).double()
+        clear = gap > eps
+        frac_near = 1.0 - float(clear.double().mean())
+        assert frac_near < 0.05, frac_near
+        dz = (z.double() - zo).abs()
+        assert bool((dz[clear] <= eps[clear]).all()), float(dz[clear].max())
+        assert bool((am[clear] == amo[clear]).all())
+        print(f"N={N}: near-barrier fraction {frac_near:.2e}, max |dz| on clear cells {float(dz[clear].max()):.3e}")
