@@ -1,18 +1,18 @@
 // d2z_cols.cuh — column passes with one lane per column (grids with N >= 32
-// and H a multiple of 16).
+// and H a multiple of the tile width).
 //
-// A tile is 16 adjacent columns x N rows.  Thread (t, c) of a CTA of 16*G
-// threads holds rows t + G*m (m < E) of column c in registers: the 16 lanes of
-// a half-warp are the 16 columns of one row, so every global load and store
-// is a whole 128-byte row segment and the data go straight from HBM into the
-// FFT registers and back, with no shared-memory staging of the tile.  Only
-// the Stockham exchanges touch shared memory: row p of column c lives at
-// p*16 + c, so a half-warp always touches 16 consecutive words (no bank
-// conflict, no swizzle), and the CTA alternates between two exchange buffers
-// so that each exchange costs one barrier.  A warp holds the two FFT lanes t
-// and G - t (lanes 0 and G/2 share warp 0); their rows ix and N - ix have the
-// same |k|, so the window is evaluated once per mirror pair and handed over
-// with one shuffle.
+// A tile is T adjacent columns x N rows (T = 16; 8 at N = 1024).  Thread
+// (t, c) of a CTA of T*G threads holds rows t + G*m (m < E) of column c in
+// registers: T lanes of a warp are the T columns of one row, so every global
+// load and store is a whole row segment (128 or 64 bytes) and the data go
+// straight from HBM into the FFT registers and back, with no shared-memory
+// staging of the tile.  Only the Stockham exchanges touch shared memory: row
+// p of column c lives at p*T + c (T = 8: with a row swizzle), so a half-warp
+// touches 16 words in distinct banks, and the CTA alternates between two
+// exchange buffers so that each exchange costs one barrier.  A warp holds FFT
+// lanes t and G - t together; their rows ix and N - ix have the same |k|, so
+// the window is evaluated once per mirror pair and handed over with one
+// shuffle.
 //
 // Modes as in k_tile: TM_FWD / TM_INV plain transforms (blockIdx.y selects a
 // slot; the next tile is loaded into registers while the current one is
@@ -25,20 +25,27 @@
 
 namespace prc {
 
+// Plan and tile width T (columns).  T = 16: the half-warps are the two FFT
+// lanes t, G - t of a mirror pair.  T = 8 (N = 1024, G = 64): a half-warp holds
+// lanes t and t + 16 (8 columns each), its partner half-warp the mirrors
+// G - t and G - t - 16; rows of 64 bytes are swizzled (PPCol::swz) so that the
+// two rows of a half-warp always sit in opposite bank halves.
 template <int N> struct CCfg { static constexpr bool on = false; };
-template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
-template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
-template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
-template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
-template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; };
-template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
-template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; };
+template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; static constexpr int T = 16; };
+template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; static constexpr int T = 16; };
+template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16; };
+template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16; };
+template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16; };
+template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16; };
+template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16; };
+template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8; };
 
 template <int N> struct CK {
   using P = typename CCfg<N>::P;
-  static constexpr int H = N / 2, T = 16, E = P::E, G = N / E, THREADS = T * G;
+  static constexpr int H = N / 2, T = CCfg<N>::T, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
   static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
+  static_assert(T == 16 || (T == 8 && G == 64 && E == 16), "lane layouts: T = 16, or T = 8 with G = 64");
   static constexpr int EH = E / 2;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
   static constexpr int BUF = N * T;                     // one exchange buffer
@@ -46,16 +53,20 @@ template <int N> struct CK {
   static constexpr int MINB = THREADS >= 512 ? 1 : (THREADS >= 256 ? 2 : 4);
 };
 
-// Two exchange buffers, column c: row p at p*16 + c.  Rows split as tp | cp
-// (disjoint bits) address as tp*16 + cp*16.
+// Two exchange buffers, column c: row p at (p ^ swz(p))*T + c.  swz is linear
+// over GF(2), so rows split as tp | cp (disjoint bits) address as
+// thread(tp) ^ ((cp ^ swz(cp))*T): one XOR per access.  T = 8 flips the row
+// parity by bits 4 and 8 of p (checked for every read and store pattern of the
+// N = 1024 plan: one wavefront per half-warp access).
 template <int T> struct PPCol {
   float2* b;
   int other;  // offset to the other buffer
-  __device__ __forceinline__ int thread(int tp) const { return tp * T; }
-  __device__ __forceinline__ float2 get(int h, int cp) const { return b[h + cp * T]; }
-  __device__ __forceinline__ void put(int h, int cp, float2 v) const { b[h + cp * T] = v; }
-  __device__ __forceinline__ float2 get_pos(int p) const { return b[p * T]; }
-  __device__ __forceinline__ void put_pos(int p, float2 v) const { b[p * T] = v; }
+  static __device__ __forceinline__ constexpr int swz(int p) { return T == 8 ? (((p >> 4) ^ (p >> 8)) & 1) : 0; }
+  __device__ __forceinline__ int thread(int tp) const { return (tp ^ swz(tp)) * T; }
+  __device__ __forceinline__ float2 get(int h, int cp) const { return b[h ^ ((cp ^ swz(cp)) * T)]; }
+  __device__ __forceinline__ void put(int h, int cp, float2 v) const { b[h ^ ((cp ^ swz(cp)) * T)] = v; }
+  __device__ __forceinline__ float2 get_pos(int p) const { return b[(p ^ swz(p)) * T]; }
+  __device__ __forceinline__ void put_pos(int p, float2 v) const { b[(p ^ swz(p)) * T] = v; }
   __device__ __forceinline__ void flip() {
     b += other;
     other = -other;
@@ -78,8 +89,14 @@ __global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a)
   if constexpr (MODE == TM_WIN || MODE == TM_ACC) stage_params(s_kr, a.kr);
   PlanRun<P>::template fill<1>(tws, a.tw);
   __syncthreads();
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, c = lane & 15;
-  const int t = (lane < 16) ? wp : (wp == 0 ? G / 2 : G - wp);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, c = lane & (T - 1);
+  int t;
+  if constexpr (T == 16) {
+    t = (lane < 16) ? wp : (wp == 0 ? G / 2 : G - wp);
+  } else {
+    const int sl = (lane >> 3) & 1;
+    t = (lane < 16) ? (sl ? wp + 16 : wp) : (sl ? 48 - wp : (wp ? 64 - wp : 32));
+  }
   PPCol<T> buf{tws + KK::TW + c, KK::BUF};
   const CtaSync sync;
   const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
@@ -130,8 +147,8 @@ __global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a)
     }
   };
   // W(|k| R_b) of all E rows: rows m > E/2 mirror rows of the partner lane
-  // (G - t, register E-1-m) or, in warp 0, of this lane (t = 0: E-m; t = G/2:
-  // E-1-m)
+  // (lane ^ 16, FFT lane G - t, register E-1-m) or of this lane (t = 0: E-m;
+  // t = G/2: E-1-m)
   // (the Taylor branch runs only in warps where some lane needs it)
   auto wvals = [&](const float (&kq)[EH + 1], float kr, float (&wv)[E]) {
     bool small = false;
@@ -154,8 +171,7 @@ __global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a)
 #pragma unroll
     for (int m = EH + 1; m < E; ++m) {
       const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
-      const float own = (t == 0) ? wv[E - m] : wv[E - 1 - m];
-      wv[m] = (wp == 0) ? own : o;
+      wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
     }
   };
 
