@@ -50,18 +50,24 @@ template <int N> struct ColLaunch<N, true> {
 template <int N, bool PAIR = PCfg<N>::on> struct C2rLaunch {
   static constexpr int THREADS = LK<N>::THREADS, NG = LK<N>::NG;
   static constexpr size_t BYTES = (size_t)LK<N>::smem_f2 * sizeof(float2);
-  static void* fn(bool = true) { return reinterpret_cast<void*>(&k_c2r_z<N>); }
+  static constexpr int NFN = 1;
+  static void* fn(int) { return reinterpret_cast<void*>(&k_c2r_z<N>); }
   static void launch(int grid, cudaStream_t st, const SweepArgs& a) { k_c2r_z<N><<<grid, THREADS, BYTES, st>>>(a); }
 };
 template <int N> struct C2rLaunch<N, true> {
   static constexpr int THREADS = PK<N>::THREADS, NG = PK<N>::NG;
   static constexpr size_t BYTES = (size_t)PK<N>::smem_f2 * sizeof(float2);
-  static void* fn(bool am = true) {
-    return am ? reinterpret_cast<void*>(&k_c2r_zp<N, true>) : reinterpret_cast<void*>(&k_c2r_zp<N, false>);
-  }
+  template <bool AM, bool SIG> static void* f() { return reinterpret_cast<void*>(&k_c2r_zp<N, AM, SIG>); }
+  static constexpr int NFN = 4;
+  static void* fn(int i) { return i == 0 ? f<false, false>() : i == 1 ? f<true, false>() : i == 2 ? f<false, true>() : f<true, true>(); }
   static void launch(int grid, cudaStream_t st, const SweepArgs& a) {
-    if (a.argmax) k_c2r_zp<N, true><<<grid, THREADS, BYTES, st>>>(a);
-    else k_c2r_zp<N, false><<<grid, THREADS, BYTES, st>>>(a);
+    if (a.sig_acc) {
+      if (a.argmax) k_c2r_zp<N, true, true><<<grid, THREADS, BYTES, st>>>(a);
+      else k_c2r_zp<N, false, true><<<grid, THREADS, BYTES, st>>>(a);
+    } else {
+      if (a.argmax) k_c2r_zp<N, true, false><<<grid, THREADS, BYTES, st>>>(a);
+      else k_c2r_zp<N, false, false><<<grid, THREADS, BYTES, st>>>(a);
+    }
   }
 };
 
@@ -90,15 +96,15 @@ template <int N> struct Launchers {
     if ((e = smem(tw, CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = smem(ta, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
-    if ((e = smem(CR::fn(true), CR::BYTES)) != cudaSuccess) return e;
-    if ((e = smem(CR::fn(false), CR::BYTES)) != cudaSuccess) return e;
+    for (int i = 0; i < CR::NFN; ++i)
+      if ((e = smem(CR::fn(i), CR::BYTES)) != cudaSuccess) return e;
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_win, tw, CL::THREADS, CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_acc, ta, CL::THREADS, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_c2r, CR::fn(), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_c2r, CR::fn(0), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r_plain, &k_c2r_plain<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_adj_z, &k_adj_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     return cudaSuccess;

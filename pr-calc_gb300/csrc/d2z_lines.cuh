@@ -62,7 +62,8 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 // copied into the other staging buffer with cp.async while the current one is
 // transformed (the NG lines of a step are one contiguous block of the slot).
 // AM: argmax wanted (a.argmax != null); its bytes are packed four to a register.
-template <int N, bool AM>
+// SIG: per-radius sums of x^2 wanted (a.sig_acc != null).
+template <int N, bool AM, bool SIG>
 __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArgs a) {
   using KK = PK<N>;
   using P = typename KK::P;
@@ -85,19 +86,17 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   const LineBuf<H> buf{gb + g * KK::gsize};
   GroupSync<G> sync(g);
   const int partner = (G - t) & (G - 1);
-  const bool want_sig = a.sig_acc != nullptr;
   const int nsteps_l = (int)((NN / NG - blockIdx.x + gridDim.x - 1) / gridDim.x);  // line groups of this CTA
   const int nb = a.nb;
   const int total = nsteps_l > 0 ? nsteps_l * nb : 0;
 
-  // copies of step i = (line group i / nb, radius i % nb) into staging buffer i & 1
-  auto issue = [&](int i) {
-    if (i < total) {
-      const long long l0 = ((long long)blockIdx.x + (long long)(i / nb) * gridDim.x) * NG;
-      const int b = i % nb;
+  // copies of step (line group lg of this CTA, radius b) into staging buffer buf
+  auto issue = [&](int lg, int b, int bi) {
+    if (lg < nsteps_l) {
+      const long long l0 = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG;
       const float2* slot = a.slots + (long long)b * a.slot_stride;
       const char* src = reinterpret_cast<const char*>(slot + l0 * H);
-      char* dst = reinterpret_cast<char*>(stage + (i & 1) * STG);
+      char* dst = reinterpret_cast<char*>(stage + bi * STG);
 #pragma unroll
       for (int q = 0; q < (STG * 8) / (16 * KK::THREADS); ++q) {
         const int off = (q * KK::THREADS + threadIdx.x) * 16;
@@ -106,18 +105,21 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
       if (t == 0) {
         const long long l = l0 + g;
         const int ix = (int)(l / N), iy = (int)(l - (l / N) * N);
-        cp_async8(nyq + (i & 1) * NG + g, slot + NN * H + (long long)iy * N + ix);
+        cp_async8(nyq + bi * NG + g, slot + NN * H + (long long)iy * N + ix);
       }
     }
     cp_async_commit();
   };
 
-  issue(0);
+  issue(0, 0, 0);
   float2 zr[E];
   uint32_t am[AM ? EH : 1];  // argmax bytes of cells 2p, 2p+1 of elements 2j (low half) and 2j+1
+  int lg = 0, b = 0;         // current step; steps run radius-fastest
   for (int i = 0; i < total; ++i) {
-    const int b = i % nb;
-    const long long l = ((long long)blockIdx.x + (long long)(i / nb) * gridDim.x) * NG + g;
+    const int bi = i & 1;
+    const int nb_next = (b + 1 < nb) ? b + 1 : 0;
+    const int lg_next = (b + 1 < nb) ? lg : lg + 1;
+    const long long l = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG + g;
     float* zline = a.zreion + l * N;
     uint16_t* aline = AM ? reinterpret_cast<uint16_t*>(a.argmax + l * N) : nullptr;
     if (b == 0) {
@@ -140,14 +142,14 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
     }
     cp_async_wait<0>();
     __syncthreads();  // step i staged for everyone; everyone is done reading buffer (i+1) & 1
-    issue(i + 1);
-    const float2* src = stage + (i & 1) * STG + g * H;
+    issue(lg_next, nb_next, bi ^ 1);
+    const float2* src = stage + bi * STG + g * H;
     float2 v[E];
     float2 mir[EH];
 #pragma unroll
     for (int m = 0; m < EH; ++m) {
       float2 x = src[t + G * m];
-      float2 xp = (m == 0 && t == 0) ? nyq[(i & 1) * NG + g] : src[H - t - G * m];
+      float2 xp = (m == 0 && t == 0) ? nyq[bi * NG + g] : src[H - t - G * m];
       if (m == 0 && t == 0) {
         x.y = 0.f;
         xp.y = 0.f;
@@ -191,9 +193,9 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
         zr[m].y = z1;
         if constexpr (AM) am[m >> 1] = (am[m >> 1] & ~(0xFF00u << sh)) | (rid << (sh + 8));
       }
-      ss = fmaf(x0, x0, fmaf(x1, x1, ss));
+      if constexpr (SIG) ss = fmaf(x0, x0, fmaf(x1, x1, ss));
     }
-    if (want_sig) {
+    if constexpr (SIG) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
       if ((threadIdx.x & 31) == 0) atomicAdd(&red[b], (double)ss);
@@ -206,9 +208,11 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
         if constexpr (AM) aline[p] = (uint16_t)(am[m >> 1] >> (16 * (m & 1)));
       }
     }
+    lg = lg_next;
+    b = nb_next;
   }
   cp_async_wait<0>();
-  if (want_sig) {
+  if constexpr (SIG) {
     __syncthreads();
     if (threadIdx.x < a.nb) atomicAdd(&a.sig_acc[a.r0 + threadIdx.x], red[threadIdx.x]);
   }
