@@ -331,6 +331,10 @@ TileSeg qseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool transpose
 void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb = 1, int r0 = 0, int first = 0) {
   TileArgs a;
   memset(&a, 0, sizeof(a));
+  if (mode == TM_WIN) {  // the window pass may use narrower tiles
+    s0.tpo = (s0.nyq ? c->N : c->H) / c->ksl.tile_w_win;
+    s1.tpo = (s1.nyq ? c->N : c->H) / c->ksl.tile_w_win;
+  }
   a.seg[0] = s0;
   a.seg[1] = s1;
   a.slot_stride = c->slot_f2;

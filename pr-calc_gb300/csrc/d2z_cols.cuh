@@ -26,26 +26,30 @@
 namespace prc {
 
 // Plan and tile width T (columns).  T = 16: the half-warps are the two FFT
-// lanes t, G - t of a mirror pair.  T = 8 (N = 1024, G = 64): a half-warp holds
-// lanes t and t + 16 (8 columns each), its partner half-warp the mirrors
-// G - t and G - t - 16; rows of 64 bytes are swizzled (PPCol::swz) so that the
-// two rows of a half-warp always sit in opposite bank halves.
+// lanes t, G - t of a mirror pair.  T = 8 (G = 32 or 64): a half-warp holds
+// lanes t and t + G/4 (8 columns each), its partner half-warp the mirrors
+// G - t and G - t - G/4; rows of 64 bytes are swizzled (PPCol::swz) so that the
+// two rows of a half-warp always sit in opposite bank halves.  The window pass
+// at N = 512 uses T = 8: two 256-thread CTAs per SM instead of one of 512, so
+// one CTA issues while the other waits at a barrier.
+// TWIN: tile width of the window pass (default T).
 template <int N> struct CCfg { static constexpr bool on = false; };
-template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; static constexpr int T = 16; };
-template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; static constexpr int T = 16; };
-template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16; };
-template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16; };
-template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16; };
-template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16; };
-template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16; };
-template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8; };
+template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
+template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
-template <int N> struct CK {
+template <int N, int T_ = CCfg<N>::T> struct CK {
   using P = typename CCfg<N>::P;
-  static constexpr int H = N / 2, T = CCfg<N>::T, E = P::E, G = N / E, THREADS = T * G;
+  static constexpr int H = N / 2, T = T_, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
   static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
-  static_assert(T == 16 || (T == 8 && G == 64 && E == 16), "lane layouts: T = 16, or T = 8 with G = 64");
+  static_assert(T == 16 || (T == 8 && E == 16 && (G == 64 || G == 32)),
+                "lane layouts: T = 16, or T = 8 with G = 32 or 64");
   static constexpr int EH = E / 2;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
   static constexpr int BUF = N * T;                     // one exchange buffer
@@ -56,12 +60,16 @@ template <int N> struct CK {
 // Two exchange buffers, column c: row p at (p ^ swz(p))*T + c.  swz is linear
 // over GF(2), so rows split as tp | cp (disjoint bits) address as
 // thread(tp) ^ ((cp ^ swz(cp))*T): one XOR per access.  T = 8 flips the row
-// parity by bits 4 and 8 of p (checked for every read and store pattern of the
-// N = 1024 plan: one wavefront per half-warp access).
-template <int T> struct PPCol {
+// parity by bits q and q + 4 of p, q = log2(G/4) (checked for every read and
+// store pattern of the N = 512 and N = 1024 plans: one wavefront per
+// half-warp access).
+template <int T, int G> struct PPCol {
   float2* b;
   int other;  // offset to the other buffer
-  static __device__ __forceinline__ constexpr int swz(int p) { return T == 8 ? (((p >> 4) ^ (p >> 8)) & 1) : 0; }
+  static constexpr int LQ = G == 64 ? 4 : 3;  // log2(G/4): the bit that tells the two lanes of a half-warp apart
+  static __device__ __forceinline__ constexpr int swz(int p) {
+    return T == 8 ? (((p >> LQ) ^ (p >> (LQ + 4))) & 1) : 0;
+  }
   __device__ __forceinline__ int thread(int tp) const { return (tp ^ swz(tp)) * T; }
   __device__ __forceinline__ float2 get(int h, int cp) const { return b[h ^ ((cp ^ swz(cp)) * T)]; }
   __device__ __forceinline__ void put(int h, int cp, float2 v) const { b[h ^ ((cp ^ swz(cp)) * T)] = v; }
@@ -77,9 +85,15 @@ struct CtaSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
+// Tile width of a mode.
+template <int N, int MODE> struct ColT {
+  static constexpr int v = MODE == TM_WIN ? CCfg<N>::TWIN : CCfg<N>::T;
+};
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a) {
-  using KK = CK<N>;
+__global__ void __launch_bounds__(CK<N, ColT<N, MODE>::v>::THREADS, CK<N, ColT<N, MODE>::v>::MINB)
+    k_col(TileArgs a) {
+  using KK = CK<N, ColT<N, MODE>::v>;
   using P = typename KK::P;
   constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, EH = KK::EH;
   constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);
@@ -94,10 +108,12 @@ __global__ void __launch_bounds__(CK<N>::THREADS, CK<N>::MINB) k_col(TileArgs a)
   if constexpr (T == 16) {
     t = (lane < 16) ? wp : (wp == 0 ? G / 2 : G - wp);
   } else {
+    // half-warp 0: lanes w, w + G/4; half-warp 1: their mirrors G - w, G - G/4 - w
+    constexpr int Q = G / 4;
     const int sl = (lane >> 3) & 1;
-    t = (lane < 16) ? (sl ? wp + 16 : wp) : (sl ? 48 - wp : (wp ? 64 - wp : 32));
+    t = (lane < 16) ? (sl ? wp + Q : wp) : (sl ? G - Q - wp : (wp ? G - wp : G / 2));
   }
-  PPCol<T> buf{tws + KK::TW + c, KK::BUF};
+  PPCol<T, G> buf{tws + KK::TW + c, KK::BUF};
   const CtaSync sync;
   const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
   const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;

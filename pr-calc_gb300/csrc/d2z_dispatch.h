@@ -13,6 +13,7 @@ struct AdjArgs;
 struct KernelSet {
   int N;
   int tile_threads, tile_w;     // threads per column-pass CTA, columns per tile
+  int tile_w_win;               // columns per tile of the window pass
   int line_threads, line_groups;  // threads per line-pass CTA, lines per CTA step
   int c2r_lines;                  // lines per CTA step of the inverse z pass
   size_t tile_smem, line_smem;  // dynamic shared memory bytes

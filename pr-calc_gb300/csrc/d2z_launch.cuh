@@ -17,8 +17,10 @@ template <int N> struct ColLaunch<N, false> {
   static constexpr int THREADS = TT::THREADS, T = TT::T;
   static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);    // one tile
   static constexpr size_t TS2 = (size_t)TT::smem2_f2 * sizeof(float2);  // two tiles (TM_WIN)
+  static constexpr int T_WIN = T;
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_tile<N, MODE>); }
   static size_t bytes(int mode) { return mode == TM_WIN ? TS2 : TS; }
+  static int threads(int) { return THREADS; }
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_tile<N, TM_FWD><<<grid, THREADS, TS, st>>>(a); break;
@@ -31,15 +33,19 @@ template <int N> struct ColLaunch<N, false> {
 
 template <int N> struct ColLaunch<N, true> {
   using CC = CK<N>;
+  using CW = CK<N, CCfg<N>::TWIN>;
   static constexpr int THREADS = CC::THREADS, T = CC::T;
+  static constexpr int THREADS_WIN = CW::THREADS, T_WIN = CW::T;
   static constexpr size_t CS = (size_t)CC::smem_f2 * sizeof(float2);
+  static constexpr size_t CSW = (size_t)CW::smem_f2 * sizeof(float2);
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_col<N, MODE>); }
-  static size_t bytes(int) { return CS; }
+  static size_t bytes(int mode) { return mode == TM_WIN ? CSW : CS; }
+  static int threads(int mode) { return mode == TM_WIN ? THREADS_WIN : THREADS; }
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_col<N, TM_FWD><<<grid, THREADS, CS, st>>>(a); break;
       case TM_INV: k_col<N, TM_INV><<<grid, THREADS, CS, st>>>(a); break;
-      case TM_WIN: k_col<N, TM_WIN><<<grid, THREADS, CS, st>>>(a); break;
+      case TM_WIN: k_col<N, TM_WIN><<<grid, THREADS_WIN, CSW, st>>>(a); break;
       default: k_col<N, TM_ACC><<<grid, THREADS, CS, st>>>(a); break;
     }
   }
@@ -101,7 +107,7 @@ template <int N> struct Launchers {
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile_win, tw, CL::THREADS, CL::bytes(TM_WIN))) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile_win, tw, CL::threads(TM_WIN), CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_acc, ta, CL::THREADS, CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r, CR::fn(0), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
@@ -128,6 +134,7 @@ template <int N> struct Launchers {
     ks.N = N;
     ks.tile_threads = CL::THREADS;
     ks.tile_w = CL::T;
+    ks.tile_w_win = CL::T_WIN;
     ks.line_threads = LL::THREADS;
     ks.line_groups = LL::NG;
     ks.c2r_lines = CR::NG;

@@ -155,6 +155,10 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     return s;
   };
   auto tile = [&](int mode, TileSeg s0, TileSeg s1, int r) {
+    if (mode == TM_WIN) {
+      s0.tpo = (s0.nyq ? N : H) / ks.tile_w_win;
+      s1.tpo = (s1.nyq ? N : H) / ks.tile_w_win;
+    }
     TileArgs a;
     memset(&a, 0, sizeof(a));
     a.seg[0] = s0;
