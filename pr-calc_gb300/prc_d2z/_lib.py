@@ -89,11 +89,12 @@ _lib = None
 
 
 def load(path: str | None = None) -> ctypes.CDLL:
-    """Load (once) the shared library; raise if it has not been built."""
+    """Load (once) the shared library; raise if it has not been built.
+    PRC_D2Z_LIB in the environment overrides the in-tree path."""
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("PRC_D2Z_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
     L = ctypes.CDLL(path)
