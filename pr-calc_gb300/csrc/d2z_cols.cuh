@@ -21,6 +21,8 @@
 // during the last radius), TM_ACC (per radius: forward transform of the slot
 // tile, accumulate W_b times it; one read-modify-write of the output).
 #pragma once
+#include <type_traits>
+
 #include "d2z_kernels.cuh"
 
 namespace prc {
@@ -32,8 +34,15 @@ namespace prc {
 // two rows of a half-warp always sit in opposite bank halves.  The window pass
 // at N = 512 uses T = 8: two 256-thread CTAs per SM instead of one of 512, so
 // one CTA issues while the other waits at a barrier.
-// TWIN: tile width of the window pass (default T).
+// TWIN / PWIN: tile width and plan of the window pass (default T / P).  (At
+// N = 512 an 8-element window plan, <8,8,8> with 64-lane groups in two
+// 512-thread CTAs of 64 registers, measured 7% slower than <16,16,2>.)
 template <int N> struct CCfg { static constexpr bool on = false; };
+template <class C, class = void> struct WinPlan { using type = typename C::P; };
+template <class C> struct WinPlan<C, decltype(void(sizeof(typename C::PWIN)))> { using type = typename C::PWIN; };
+template <class P> struct FirstRadix;
+template <int E, int R0, int... R> struct FirstRadix<Plan<E, R0, R...>> { static constexpr int v = R0; };
+constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16, TWIN = 16; };
@@ -43,18 +52,18 @@ template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<1
 template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
 template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
-template <int N, int T_ = CCfg<N>::T> struct CK {
-  using P = typename CCfg<N>::P;
+template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
+  using P = P_;
   static constexpr int H = N / 2, T = T_, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
   static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
-  static_assert(T == 16 || (T == 8 && E == 16 && (G == 64 || G == 32)),
-                "lane layouts: T = 16, or T = 8 with G = 32 or 64");
+  static_assert(T == 16 || (T == 8 && (G == 64 || G == 32)), "lane layouts: T = 16, or T = 8 with G = 32 or 64");
   static constexpr int EH = E / 2;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
   static constexpr int BUF = N * T;                     // one exchange buffer
   static constexpr int smem_f2 = TW + 2 * BUF;
-  static constexpr int MINB = THREADS >= 512 ? 1 : (THREADS >= 256 ? 2 : 4);
+  // resident CTAs per SM the register budget is sized for (E = 8: two 512-thread CTAs)
+  static constexpr int MINB = THREADS >= 512 ? (E <= 8 ? 2 : 1) : (THREADS >= 256 ? 2 : 4);
 };
 
 // Two exchange buffers, column c: row p at (p ^ swz(p))*T + c.  swz is linear
@@ -62,13 +71,14 @@ template <int N, int T_ = CCfg<N>::T> struct CK {
 // thread(tp) ^ ((cp ^ swz(cp))*T): one XOR per access.  T = 8 flips the row
 // parity by bits q and q + 4 of p, q = log2(G/4) (checked for every read and
 // store pattern of the N = 512 and N = 1024 plans: one wavefront per
-// half-warp access).
-template <int T, int G> struct PPCol {
+// half-warp access); q + 4 is q + log2(first radix) in general.
+template <int T, int G, int R0> struct PPCol {
   float2* b;
   int other;  // offset to the other buffer
-  static constexpr int LQ = G == 64 ? 4 : 3;  // log2(G/4): the bit that tells the two lanes of a half-warp apart
+  static constexpr int LQ = ilog2(G / 4);      // the bit that tells the two lanes of a half-warp apart
+  static constexpr int LS = LQ + ilog2(R0);    // where the first stage's stores move that bit
   static __device__ __forceinline__ constexpr int swz(int p) {
-    return T == 8 ? (((p >> LQ) ^ (p >> (LQ + 4))) & 1) : 0;
+    return T == 8 ? (((p >> LQ) ^ (p >> LS)) & 1) : 0;
   }
   __device__ __forceinline__ int thread(int tp) const { return (tp ^ swz(tp)) * T; }
   __device__ __forceinline__ float2 get(int h, int cp) const { return b[h ^ ((cp ^ swz(cp)) * T)]; }
@@ -85,15 +95,18 @@ struct CtaSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
-// Tile width of a mode.
+// Tile width and plan of a mode.
 template <int N, int MODE> struct ColT {
   static constexpr int v = MODE == TM_WIN ? CCfg<N>::TWIN : CCfg<N>::T;
 };
+template <int N, int MODE> struct ColK {
+  using type = CK<N, ColT<N, MODE>::v,
+                  typename std::conditional<MODE == TM_WIN, typename WinPlan<CCfg<N>>::type, typename CCfg<N>::P>::type>;
+};
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(CK<N, ColT<N, MODE>::v>::THREADS, CK<N, ColT<N, MODE>::v>::MINB)
-    k_col(TileArgs a) {
-  using KK = CK<N, ColT<N, MODE>::v>;
+__global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::type::MINB) k_col(TileArgs a) {
+  using KK = typename ColK<N, MODE>::type;
   using P = typename KK::P;
   constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, EH = KK::EH;
   constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);
@@ -113,7 +126,7 @@ __global__ void __launch_bounds__(CK<N, ColT<N, MODE>::v>::THREADS, CK<N, ColT<N
     const int sl = (lane >> 3) & 1;
     t = (lane < 16) ? (sl ? wp + Q : wp) : (sl ? G - Q - wp : (wp ? G - wp : G / 2));
   }
-  PPCol<T, G> buf{tws + KK::TW + c, KK::BUF};
+  PPCol<T, G, FirstRadix<P>::v> buf{tws + KK::TW + c, KK::BUF};
   const CtaSync sync;
   const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
   const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;

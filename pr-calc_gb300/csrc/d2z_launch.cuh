@@ -33,7 +33,7 @@ template <int N> struct ColLaunch<N, false> {
 
 template <int N> struct ColLaunch<N, true> {
   using CC = CK<N>;
-  using CW = CK<N, CCfg<N>::TWIN>;
+  using CW = typename ColK<N, TM_WIN>::type;
   static constexpr int THREADS = CC::THREADS, T = CC::T;
   static constexpr int THREADS_WIN = CW::THREADS, T_WIN = CW::T;
   static constexpr size_t CS = (size_t)CC::smem_f2 * sizeof(float2);
