@@ -331,9 +331,10 @@ TileSeg qseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool transpose
 void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb = 1, int r0 = 0, int first = 0) {
   TileArgs a;
   memset(&a, 0, sizeof(a));
-  if (mode == TM_WIN) {  // the window pass may use narrower tiles
-    s0.tpo = (s0.nyq ? c->N : c->H) / c->ksl.tile_w_win;
-    s1.tpo = (s1.nyq ? c->N : c->H) / c->ksl.tile_w_win;
+  if (mode == TM_WIN || mode == TM_ACC) {  // these passes may use narrower tiles
+    const int tw = mode == TM_WIN ? c->ksl.tile_w_win : c->ksl.tile_w_acc;
+    s0.tpo = (s0.nyq ? c->N : c->H) / tw;
+    s1.tpo = (s1.nyq ? c->N : c->H) / tw;
   }
   a.seg[0] = s0;
   a.seg[1] = s1;

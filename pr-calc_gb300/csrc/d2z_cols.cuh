@@ -1,7 +1,8 @@
 // d2z_cols.cuh — column passes with one lane per column (grids with N >= 32
 // and H a multiple of the tile width).
 //
-// A tile is T adjacent columns x N rows (T = 16; 8 at N = 1024).  Thread
+// A tile is T adjacent columns x N rows (T = 16; 8 in the window pass at
+// N = 512 and in every pass at N = 1024).  Thread
 // (t, c) of a CTA of T*G threads holds rows t + G*m (m < E) of column c in
 // registers: T lanes of a warp are the T columns of one row, so every global
 // load and store is a whole row segment (128 or 64 bytes) and the data go
@@ -50,6 +51,9 @@ template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<1
 template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
+// N = 1024: 64 lanes x 8 columns in every pass.  (Plain passes on 32 lanes x
+// 16 columns with 32 elements a lane -- 128-byte rows, but one exchange buffer
+// and no register prefetch -- measured 1% slower over the whole step.)
 template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
 template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
@@ -61,7 +65,10 @@ template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK 
   static constexpr int EH = E / 2;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;  // stage twiddles, even for alignment
   static constexpr int BUF = N * T;                     // one exchange buffer
-  static constexpr int smem_f2 = TW + 2 * BUF;
+  // two exchange buffers (one barrier per exchange) when they fit in shared
+  // memory, else one (two barriers per exchange: 1024 rows x 16 columns)
+  static constexpr bool PP = (TW + 2 * BUF) * 8 <= 200 * 1024;
+  static constexpr int smem_f2 = TW + (PP ? 2 : 1) * BUF;
   // resident CTAs per SM the register budget is sized for (E = 8: two 512-thread CTAs)
   static constexpr int MINB = THREADS >= 512 ? (E <= 8 ? 2 : 1) : (THREADS >= 256 ? 2 : 4);
 };
@@ -95,13 +102,19 @@ struct CtaSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
-// Tile width and plan of a mode.
+// Tile width and plan of a mode: the window pass uses TWIN / PWIN, and so
+// does the accumulate mode when the plain plan holds more than 16 elements a
+// lane (its accumulator would not fit beside them).
+template <int N, int MODE> struct ColUsesWin {
+  static constexpr bool v = MODE == TM_WIN || (MODE == TM_ACC && CCfg<N>::P::E > 16);
+};
 template <int N, int MODE> struct ColT {
-  static constexpr int v = MODE == TM_WIN ? CCfg<N>::TWIN : CCfg<N>::T;
+  static constexpr int v = ColUsesWin<N, MODE>::v ? CCfg<N>::TWIN : CCfg<N>::T;
 };
 template <int N, int MODE> struct ColK {
   using type = CK<N, ColT<N, MODE>::v,
-                  typename std::conditional<MODE == TM_WIN, typename WinPlan<CCfg<N>>::type, typename CCfg<N>::P>::type>;
+                  typename std::conditional<ColUsesWin<N, MODE>::v, typename WinPlan<CCfg<N>>::type,
+                                            typename CCfg<N>::P>::type>;
 };
 
 template <int N, int MODE>
@@ -204,7 +217,7 @@ __global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::t
     }
   };
 
-  if constexpr (MODE == TM_FWD || MODE == TM_INV) {
+  if constexpr ((MODE == TM_FWD || MODE == TM_INV) && E <= 16) {
     float2 v[E], nx[E];
     int ti = blockIdx.x;
     if (ti < tiles) {
@@ -218,10 +231,20 @@ __global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::t
         const Where wn = where(tn);
         gload(wn.sg.in + wn.off + yoff, wn.sg.row_stride, nx);
       }
-      PlanRun<P>::template run<INV, true>(v, buf, t, tws, sync);
+      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
       gstore(w, w.sg.out + yoff, v);
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = nx[m];
+    }
+  } else if constexpr (MODE == TM_FWD || MODE == TM_INV) {
+    // 32 elements a lane: no room for a prefetch; 32 independent loads per
+    // lane keep enough bytes in flight on their own
+    for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+      const Where w = where(ti);
+      float2 v[E];
+      gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
+      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
+      gstore(w, w.sg.out + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
     float2 raw[E];
@@ -248,7 +271,7 @@ __global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::t
             gload(wn.sg.in + wn.off, wn.sg.row_stride, raw);
           }
         }
-        PlanRun<P>::template run<true, true>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<true, KK::PP>(v, buf, t, tws, sync);
         gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
@@ -266,7 +289,7 @@ __global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::t
       for (int b = 0; b < a.nb; ++b) {
         float2 v[E];
         gload(w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride, v);
-        PlanRun<P>::template run<false, true>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
         float wv[E];
         wvals(kq, s_kr[b], wv);
 #pragma unroll

@@ -14,6 +14,7 @@ struct KernelSet {
   int N;
   int tile_threads, tile_w;     // threads per column-pass CTA, columns per tile
   int tile_w_win;               // columns per tile of the window pass
+  int tile_w_acc;               // columns per tile of the accumulate pass (adjoint)
   int line_threads, line_groups;  // threads per line-pass CTA, lines per CTA step
   int c2r_lines;                  // lines per CTA step of the inverse z pass
   size_t tile_smem, line_smem;  // dynamic shared memory bytes

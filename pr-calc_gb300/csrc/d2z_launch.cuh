@@ -21,6 +21,7 @@ template <int N> struct ColLaunch<N, false> {
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_tile<N, MODE>); }
   static size_t bytes(int mode) { return mode == TM_WIN ? TS2 : TS; }
   static int threads(int) { return THREADS; }
+  static constexpr int T_ACC = T;
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_tile<N, TM_FWD><<<grid, THREADS, TS, st>>>(a); break;
@@ -32,21 +33,23 @@ template <int N> struct ColLaunch<N, false> {
 };
 
 template <int N> struct ColLaunch<N, true> {
-  using CC = CK<N>;
+  using CC = typename ColK<N, TM_INV>::type;
   using CW = typename ColK<N, TM_WIN>::type;
+  using CA = typename ColK<N, TM_ACC>::type;
   static constexpr int THREADS = CC::THREADS, T = CC::T;
-  static constexpr int THREADS_WIN = CW::THREADS, T_WIN = CW::T;
+  static constexpr int T_WIN = CW::T, T_ACC = CA::T;
   static constexpr size_t CS = (size_t)CC::smem_f2 * sizeof(float2);
   static constexpr size_t CSW = (size_t)CW::smem_f2 * sizeof(float2);
+  static constexpr size_t CSA = (size_t)CA::smem_f2 * sizeof(float2);
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_col<N, MODE>); }
-  static size_t bytes(int mode) { return mode == TM_WIN ? CSW : CS; }
-  static int threads(int mode) { return mode == TM_WIN ? THREADS_WIN : THREADS; }
+  static size_t bytes(int mode) { return mode == TM_WIN ? CSW : mode == TM_ACC ? CSA : CS; }
+  static int threads(int mode) { return mode == TM_WIN ? CW::THREADS : mode == TM_ACC ? CA::THREADS : THREADS; }
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_col<N, TM_FWD><<<grid, THREADS, CS, st>>>(a); break;
       case TM_INV: k_col<N, TM_INV><<<grid, THREADS, CS, st>>>(a); break;
-      case TM_WIN: k_col<N, TM_WIN><<<grid, THREADS_WIN, CSW, st>>>(a); break;
-      default: k_col<N, TM_ACC><<<grid, THREADS, CS, st>>>(a); break;
+      case TM_WIN: k_col<N, TM_WIN><<<grid, CW::THREADS, CSW, st>>>(a); break;
+      default: k_col<N, TM_ACC><<<grid, CA::THREADS, CSA, st>>>(a); break;
     }
   }
 };
@@ -108,7 +111,7 @@ template <int N> struct Launchers {
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_win, tw, CL::threads(TM_WIN), CL::bytes(TM_WIN))) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile_acc, ta, CL::THREADS, CL::bytes(TM_ACC))) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_tile_acc, ta, CL::threads(TM_ACC), CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r, CR::fn(0), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r_plain, &k_c2r_plain<N>, LL::THREADS, LS)) != cudaSuccess) return e;
@@ -135,6 +138,7 @@ template <int N> struct Launchers {
     ks.tile_threads = CL::THREADS;
     ks.tile_w = CL::T;
     ks.tile_w_win = CL::T_WIN;
+    ks.tile_w_acc = CL::T_ACC;
     ks.line_threads = LL::THREADS;
     ks.line_groups = LL::NG;
     ks.c2r_lines = CR::NG;

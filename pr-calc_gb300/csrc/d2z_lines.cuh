@@ -184,14 +184,22 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
     for (int m = 0; m < E; ++m) {
       const float x0 = v[m].x, x1 = v[m].y;
       const float z0 = fmaf(a.as, x0, cb), z1 = fmaf(a.as, x1, cb);
-      const int sh = 16 * (m & 1);
-      if (z0 > zr[m].x) {
-        zr[m].x = z0;
-        if constexpr (AM) am[m >> 1] = (am[m >> 1] & ~(0xFFu << sh)) | (rid << sh);
-      }
-      if (z1 > zr[m].y) {
-        zr[m].y = z1;
-        if constexpr (AM) am[m >> 1] = (am[m >> 1] & ~(0xFF00u << sh)) | (rid << (sh + 8));
+      if constexpr (AM) {
+        const int sh = 16 * (m & 1);
+        if (z0 > zr[m].x) {
+          zr[m].x = z0;
+          am[m >> 1] = (am[m >> 1] & ~(0xFFu << sh)) | (rid << sh);
+        }
+        if (z1 > zr[m].y) {
+          zr[m].y = z1;
+          am[m >> 1] = (am[m >> 1] & ~(0xFF00u << sh)) | (rid << (sh + 8));
+        }
+      } else {
+        // without the argmax the strict update is a max: fmaxf keeps zr when
+        // z is NaN (the barrier of a radius that never wins) and equal values
+        // are the same number
+        zr[m].x = fmaxf(zr[m].x, z0);
+        zr[m].y = fmaxf(zr[m].y, z1);
       }
       if constexpr (SIG) ss = fmaf(x0, x0, fmaf(x1, x1, ss));
     }
