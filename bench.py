@@ -453,7 +453,7 @@ def main():
     ap.add_argument("--ref-radii", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
-    ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--streams", type=int, default=2)
     args = ap.parse_args()
     _use_config(args.config)
     if args.n == 0:
