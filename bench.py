@@ -219,7 +219,15 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(dev)
     N = args.n
     p, cl = _params(N)
-    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=args.batch, argmax=False)
+    tuned = None
+    if args.batch == 0:
+        # radius batch and window-pass variant from the autotuner (cached per device)
+        from prc_d2z import autotune
+        tuned = autotune.tuned(N, NR)
+    B_use = tuned[0] if tuned else args.batch
+    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=B_use, argmax=False)
+    if tuned:
+        ctx.tune(0, tuned[1])
     t = ctx.tables
     delta = fields.gaussian_field(N, p.BoxSize, seed=1 + rank, backend="torch", device=dev).contiguous()
     zreion = torch.empty_like(delta)
@@ -271,7 +279,7 @@ def run_ours(args, rank, world, local_rank):
         return
     # roofline of the dominant kernel
     peak, peak_kind = _peaks()
-    B = min(args.batch or 8, NR)
+    B = min(B_use, NR)
     sweeps = math.ceil(NR / B)
     dom = max((k for k in prof if prof[k][1] > 0), key=lambda k: prof[k][0])
     tot_ms, n_l = prof[dom]
@@ -284,6 +292,11 @@ def run_ours(args, rank, world, local_rank):
         bytes_launch = _algo_bytes(dom, N, 1, True) or 0
     achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
     traffic = _traffic(dom, N)
+    if traffic is not None and dom in ("win_x", "col_inv", "c2r_z"):
+        # the committed summaries are for a radius batch of 8: scale by the units processed
+        s8 = math.ceil(NR / 8)
+        b8 = sum(_algo_bytes(dom, N, min(8, NR - s * 8), s == 0) for s in range(s8)) / s8
+        traffic *= bytes_launch / b8
     rl = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
           "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
           "bytes_per_launch": bytes_launch, "ms_per_launch": per_launch_ms,
@@ -297,6 +310,7 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox4x32-10 + BBKS, seed 1+rank)",
         "config": {"workload": f"plain delta2zreion {N}^3, {p.BoxSize:g} Mpc/h, {NR} radii", "N": N,
                    "radii": NR, "box_mpc_h": p.BoxSize, "zeta": ZETA, "radius_batch": B,
+                   "win_variant": tuned[1] if tuned else 0, "autotuned": tuned is not None,
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * N ** 3, "d2h_bytes_per_step": 4 * N ** 3},
         "gpu_launches": launches,
@@ -331,7 +345,9 @@ def _cfg_box(N, nr, seed, zeta, box=None, rmax=RMAX):
 
 def run_batched(args):
     """96 realisations, grids 64/96/128/192/256 at 1.5 Mpc/h cells, 24-48 radii
-    each: per-box loop of the plain path vs one captured-graph batch launch."""
+    each: per-box loop of the plain path vs one captured-graph batch launch.
+    Both use the autotuned radius batch and window-pass variant of each grid
+    size (prc_d2z.autotune); the batch also picks its stream count by timing."""
     import torch
 
     import prc_d2z
@@ -348,17 +364,38 @@ def run_batched(args):
     work = sum(b["N"] ** 3 * len(b["radii_mpc"]) for b in boxes)
     outs_loop = [torch.empty_like(d) for d in deltas]
     outs_batch = [torch.empty_like(d) for d in deltas]
+    # autotuned radius batch and window-pass variant per grid size (cached)
+    from prc_d2z import autotune
+    nr_rep = int(np.median(nrs))
+    tuning = {int(N): autotune.tuned(int(N), nr_rep) for N in sorted(set(sizes))}
+    for b in boxes:
+        b["radius_batch"] = tuning[b["N"]][0]
     ctxs = [prc_d2z.Delta2Zreion(b["N"], b["box_mpc"], b["radii_mpc"], b["barrier_b"], b["barrier_a"],
-                                 b["growth_init"], argmax=False) for b in boxes]
+                                 b["growth_init"], radius_batch=b["radius_batch"], argmax=False) for b in boxes]
+    for c, b in zip(ctxs, boxes):
+        c.tune(0, tuning[b["N"]][1])
 
     def loop():
         for c, d, o in zip(ctxs, deltas, outs_loop):
             c.forward(d, zreion=o, want_argmax=False)
 
-    batch = prc_d2z.Batch(boxes, n_streams=args.streams)
+    def make_batch(n_streams):
+        bt = prc_d2z.Batch(boxes, n_streams=n_streams)
+        for i, b in enumerate(boxes):
+            bt.tune(i, 0, tuning[b["N"]][1])
+        return bt
+
+    def run_batch(bt):
+        bt.forward(deltas, outs_batch, use_graph=True)
+
+    stream_ms = None
+    streams = args.streams
+    if streams <= 0:
+        streams, stream_ms = autotune.tune_batch_streams(make_batch, run_batch, streams=(1, 2, 4))
+    batch = make_batch(streams)
 
     def batched():
-        batch.forward(deltas, outs_batch, use_graph=True)
+        run_batch(batch)
 
     res = {}
     for name, fn in (("loop", loop), ("batched", batched)):
@@ -382,7 +419,9 @@ def run_batched(args):
         "data": "synthetic (Philox4x32-10 + BBKS, seeds 1000..1095)",
         "config": {"workload": "batched: 96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
                                "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
-                   "streams": args.streams, "graph": True},
+                   "streams": streams, "graph": True,
+                   "autotuned": {str(N): {"radius_batch": B, "win_variant": v} for N, (B, v) in tuning.items()},
+                   "streams_ms": stream_ms},
         "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3)},
         "speedup_vs_loop": ms_loop / ms_b, "identical_to_loop": bool(same),
         "gpu_launches": batch.launches(), "clocks": res["batched"][1]}), flush=True)
@@ -453,7 +492,7 @@ def main():
     ap.add_argument("--ref-radii", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
-    ap.add_argument("--streams", type=int, default=2)
+    ap.add_argument("--streams", type=int, default=0, help="batched: streams (0: autotuned)")
     args = ap.parse_args()
     _use_config(args.config)
     if args.n == 0:

@@ -105,6 +105,17 @@ typedef struct {
   void*         stream;           /* cudaStream_t; NULL = default stream        */
 } prc_d2z_desc;
 
+/* Tuning knobs (no counterpart in the reference, whose FFTW plans are
+ * chosen by FFTW).  prc_d2z_win_variants: how many window-pass variants (tile
+ * width and radix plan) are compiled for grid side N (0: N unsupported).
+ * prc_d2z_tune: the radius batch (radii per sweep, 0 = keep; a larger batch
+ * reallocates the radius slots) and the window-pass variant of a context;
+ * results do not depend on either beyond float rounding of the transform.
+ * prc_d2z_batch_tune: the same for box `box` of a batch (the next forward
+ * re-captures its graph).  prc_d2z.autotune picks both by timing. */
+int prc_d2z_win_variants(int N);
+int prc_d2z_tune(prc_d2z_ctx* ctx, int radius_batch, int win_variant);
+
 /* Synthetic input fields (the producer of delta_lin; the role of the ics
  * generator, grf_ics.C:8-112, whose drand48 + Marsaglia-polar stream is
  * sequential by construction and is replaced by a counter-based one).
@@ -235,6 +246,7 @@ int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
  * No reference counterpart: the reference processes one box per run. */
 typedef struct prc_d2z_batch prc_d2z_batch;
 int prc_d2z_batch_create(int n_boxes, const prc_d2z_desc* descs, int n_streams, prc_d2z_batch** out);
+int prc_d2z_batch_tune(prc_d2z_batch* batch, int box, int radius_batch, int win_variant);
 int prc_d2z_batch_forward(prc_d2z_batch* batch, const float* const* delta, float* const* zreion,
                           uint8_t* const* argmax, int use_graph);
 int prc_d2z_batch_launches(prc_d2z_batch* batch, int* n);

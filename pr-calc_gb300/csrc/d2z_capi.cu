@@ -185,6 +185,8 @@ using namespace prc;
 
 struct prc_d2z_ctx {
   int N = 0, H = 0, nr = 0, B = 0, flags = 0, dev = 0, sms = 0;
+  int win_var = 0;   // window-pass variant (prc_d2z_tune)
+  int slots_b = 0;   // radius slots allocated
   long long NN = 0, slot_f2 = 0;
   double box = 0, A = 0, dinit = 1;
   std::vector<double> R, Bb;
@@ -332,7 +334,7 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
   TileArgs a;
   memset(&a, 0, sizeof(a));
   if (mode == TM_WIN || mode == TM_ACC) {  // these passes may use narrower tiles
-    const int tw = mode == TM_WIN ? c->ksl.tile_w_win : c->ksl.tile_w_acc;
+    const int tw = mode == TM_WIN ? c->ksl.tile_w_winv[c->win_var] : c->ksl.tile_w_acc;
     s0.tpo = (s0.nyq ? c->N : c->H) / tw;
     s1.tpo = (s1.nyq ? c->N : c->H) / tw;
   }
@@ -342,10 +344,11 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
   a.tw = c->tw;
   a.nb = nb;
   a.first = first;
+  a.win_var = c->win_var;
   if (mode == TM_WIN || mode == TM_ACC)
     for (int b = 0; b < nb; ++b) a.kr[b] = c->kr[r0 + b];
   const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
-  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : (mode == TM_WIN) ? c->ksl.occ_tile_win : c->ksl.occ_tile;
+  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : (mode == TM_WIN) ? c->ksl.occ_winv[c->win_var] : c->ksl.occ_tile;
   dim3 grid(grid_for(tiles, 1, occ, c->sms), gy, 1);
   const int kind = mode == TM_FWD ? PRC_KIND_COL_FWD
                  : mode == TM_INV ? PRC_KIND_COL_INV
@@ -502,6 +505,7 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
   int B = d->radius_batch ? d->radius_batch : 8;
   if (B > c->nr) B = c->nr;
   c->B = B;
+  c->slots_b = B;
   const double dk = 2.0 * M_PI / d->box_mpc;
   const double n3 = (double)d->N * d->N * d->N;
   c->as = (float)(d->barrier_a / n3);
@@ -912,6 +916,49 @@ int prc_d2z_set_barrier(prc_d2z_ctx* c, const double* barrier_b, double barrier_
     c->Bb[r] = barrier_b[r];
     c->cb[r] = (float)(barrier_a * barrier_b[r] - 1.0);
   }
+  return PRC_OK;
+}
+
+int prc_d2z_win_variants(int N) {
+  const KernelSet* ks = kernel_set(N);
+  return ks ? ks->n_win_var : 0;
+}
+
+int prc_d2z_tune(prc_d2z_ctx* c, int radius_batch, int win_variant) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (win_variant < 0 || win_variant >= c->ksl.n_win_var)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_tune: window variant %d outside 0..%d for N=%d", win_variant,
+                    c->ksl.n_win_var - 1, c->N);
+  if (radius_batch < 0 || radius_batch > kMaxBatch)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_tune: radius_batch must be 0..%d", kMaxBatch);
+  int B = radius_batch ? radius_batch : c->B;
+  if (B > c->nr) B = c->nr;
+  if (B > c->slots_b) {  // more radius slots: a new, larger allocation
+    if ((st = set_device(c)) != PRC_OK) return st;
+    PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_tune");
+    float2* ns = nullptr;
+    if ((st = dalloc(&ns, (size_t)c->slot_f2 * B, "radius slots")) != PRC_OK) return st;
+    cudaFree(c->slots);
+    c->slots = ns;
+    c->slots_b = B;
+  }
+  c->B = B;
+  c->win_var = win_variant;
+  return PRC_OK;
+}
+
+int prc_d2z_batch_tune(prc_d2z_batch* b, int box, int radius_batch, int win_variant) {
+  if (!b) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_tune: null batch");
+  if (box < 0 || box >= b->n) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_tune: box %d outside 0..%d", box, b->n - 1);
+  int st;
+  if ((st = prc_d2z_tune(b->ctx[box], radius_batch, win_variant)) != PRC_OK) return st;
+  // the captured graph holds the old launches
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->key.clear();
   return PRC_OK;
 }
 

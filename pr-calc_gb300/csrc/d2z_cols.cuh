@@ -102,24 +102,36 @@ struct CtaSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
-// Tile width and plan of a mode: the window pass uses TWIN / PWIN, and so
-// does the accumulate mode when the plain plan holds more than 16 elements a
-// lane (its accumulator would not fit beside them).
+// Window-pass variants (tile width, plan) the autotuner chooses among.
+// Variant 0 is the default (TWIN / PWIN); up to kWinVariants per grid size.
+constexpr int kWinVariants = 3;
+template <int N, int V> struct WinVar { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
+template <int N> struct WinVar<N, 0> {
+  static constexpr bool on = CCfg<N>::on;
+  static constexpr int T = CCfg<N>::TWIN;
+  using P = typename WinPlan<CCfg<N>>::type;
+};
+template <> struct WinVar<128, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
+template <> struct WinVar<256, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<256, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<512, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
+template <> struct WinVar<512, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+
+// Tile width and plan of a mode: the window pass uses its variant V, and the
+// accumulate mode uses variant 0 of the window pass when the plain plan holds
+// more than 16 elements a lane (its accumulator would not fit beside them).
 template <int N, int MODE> struct ColUsesWin {
   static constexpr bool v = MODE == TM_WIN || (MODE == TM_ACC && CCfg<N>::P::E > 16);
 };
-template <int N, int MODE> struct ColT {
-  static constexpr int v = ColUsesWin<N, MODE>::v ? CCfg<N>::TWIN : CCfg<N>::T;
-};
-template <int N, int MODE> struct ColK {
-  using type = CK<N, ColT<N, MODE>::v,
-                  typename std::conditional<ColUsesWin<N, MODE>::v, typename WinPlan<CCfg<N>>::type,
-                                            typename CCfg<N>::P>::type>;
+template <int N, int MODE, int V> struct ColK {
+  static constexpr int VV = MODE == TM_WIN ? V : 0;
+  using type = typename std::conditional<ColUsesWin<N, MODE>::v, CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P>,
+                                         CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
 };
 
-template <int N, int MODE>
-__global__ void __launch_bounds__(ColK<N, MODE>::type::THREADS, ColK<N, MODE>::type::MINB) k_col(TileArgs a) {
-  using KK = typename ColK<N, MODE>::type;
+template <int N, int MODE, int V = 0>
+__global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE, V>::type::MINB) k_col(TileArgs a) {
+  using KK = typename ColK<N, MODE, V>::type;
   using P = typename KK::P;
   constexpr int H = N / 2, E = KK::E, G = KK::G, T = KK::T, EH = KK::EH;
   constexpr bool INV = (MODE == TM_INV || MODE == TM_WIN);

@@ -6,6 +6,8 @@
 
 namespace prc {
 
+constexpr int kMaxWinVariants = 3;  // window-pass variants per grid size (autotuned)
+
 struct TileArgs;
 struct SweepArgs;
 struct AdjArgs;
@@ -13,7 +15,9 @@ struct AdjArgs;
 struct KernelSet {
   int N;
   int tile_threads, tile_w;     // threads per column-pass CTA, columns per tile
-  int tile_w_win;               // columns per tile of the window pass
+  int tile_w_win;               // columns per tile of the window pass (variant 0)
+  int n_win_var;                // window-pass variants compiled for this N
+  int tile_w_winv[kMaxWinVariants], occ_winv[kMaxWinVariants];  // per variant
   int tile_w_acc;               // columns per tile of the accumulate pass (adjoint)
   int line_threads, line_groups;  // threads per line-pass CTA, lines per CTA step
   int c2r_lines;                  // lines per CTA step of the inverse z pass

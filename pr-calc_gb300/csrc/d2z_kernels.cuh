@@ -112,6 +112,7 @@ struct TileArgs {
   long long slot_stride;   // plain: per blockIdx.y; WIN: per radius (out); ACC: per radius (in)
   const float2* tw;        // N-entry table e^{+2 pi i k/N}
   int nb, first;
+  int win_var;             // window-pass variant (host-side launch choice)
   float kr[kMaxBatch];     // dk * R_b
 };
 

@@ -8,6 +8,8 @@
 
 namespace prc {
 
+static_assert(kWinVariants == kMaxWinVariants, "window variant table size");
+
 // Column passes: k_col (one lane per column) where CCfg<N> has a plan, else
 // k_tile (shared-memory staged tiles).
 template <int N, bool COL = CCfg<N>::on> struct ColLaunch;
@@ -17,11 +19,20 @@ template <int N> struct ColLaunch<N, false> {
   static constexpr int THREADS = TT::THREADS, T = TT::T;
   static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);    // one tile
   static constexpr size_t TS2 = (size_t)TT::smem2_f2 * sizeof(float2);  // two tiles (TM_WIN)
-  static constexpr int T_WIN = T;
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_tile<N, MODE>); }
   static size_t bytes(int mode) { return mode == TM_WIN ? TS2 : TS; }
   static int threads(int) { return THREADS; }
   static constexpr int T_ACC = T;
+  // one window variant: the staged tile kernel
+  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr) {
+    if (v == 0) {
+      if (f) *f = reinterpret_cast<void*>(&k_tile<N, TM_WIN>);
+      if (thr) *thr = THREADS;
+      if (by) *by = TS2;
+      if (tw) *tw = T;
+    }
+    return 1;
+  }
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_tile<N, TM_FWD><<<grid, THREADS, TS, st>>>(a); break;
@@ -33,22 +44,58 @@ template <int N> struct ColLaunch<N, false> {
 };
 
 template <int N> struct ColLaunch<N, true> {
-  using CC = typename ColK<N, TM_INV>::type;
-  using CW = typename ColK<N, TM_WIN>::type;
-  using CA = typename ColK<N, TM_ACC>::type;
+  using CC = typename ColK<N, TM_INV, 0>::type;
+  using CA = typename ColK<N, TM_ACC, 0>::type;
   static constexpr int THREADS = CC::THREADS, T = CC::T;
-  static constexpr int T_WIN = CW::T, T_ACC = CA::T;
+  static constexpr int T_ACC = CA::T;
   static constexpr size_t CS = (size_t)CC::smem_f2 * sizeof(float2);
-  static constexpr size_t CSW = (size_t)CW::smem_f2 * sizeof(float2);
   static constexpr size_t CSA = (size_t)CA::smem_f2 * sizeof(float2);
+  // window-pass variant v (when compiled for this N)
+  template <int V> struct Win {
+    static constexpr bool on = WinVar<N, V>::on;
+    using K = typename ColK<N, TM_WIN, V>::type;
+  };
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_col<N, MODE>); }
-  static size_t bytes(int mode) { return mode == TM_WIN ? CSW : mode == TM_ACC ? CSA : CS; }
-  static int threads(int mode) { return mode == TM_WIN ? CW::THREADS : mode == TM_ACC ? CA::THREADS : THREADS; }
+  static size_t bytes(int mode) { return mode == TM_ACC ? CSA : CS; }
+  static int threads(int mode) { return mode == TM_ACC ? CA::THREADS : THREADS; }
+  template <int V> static void win_info(int v, int* n, void** f, int* thr, size_t* by, int* tw) {
+    if constexpr (V < kWinVariants) {
+      if constexpr (Win<V>::on) {
+        if (v == V) {
+          *f = reinterpret_cast<void*>(&k_col<N, TM_WIN, V>);
+          *thr = Win<V>::K::THREADS;
+          *by = (size_t)Win<V>::K::smem_f2 * sizeof(float2);
+          *tw = Win<V>::K::T;
+        }
+        *n = V + 1;
+      }
+      win_info<V + 1>(v, n, f, thr, by, tw);
+    }
+  }
+  // number of window variants and, for variant v, its kernel, threads, bytes, tile width
+  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr) {
+    int n = 0, t0 = 0, w0 = 0;
+    void* f0 = nullptr;
+    size_t b0 = 0;
+    win_info<0>(v, &n, f ? f : &f0, thr ? thr : &t0, by ? by : &b0, tw ? tw : &w0);
+    return n;
+  }
+  template <int V> static void launch_win(int v, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    if constexpr (V < kWinVariants) {
+      if constexpr (Win<V>::on) {
+        if (v == V) {
+          k_col<N, TM_WIN, V><<<grid, Win<V>::K::THREADS, (size_t)Win<V>::K::smem_f2 * sizeof(float2), st>>>(a);
+          return;
+        }
+      }
+      launch_win<V + 1>(v, grid, st, a);
+    }
+  }
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_col<N, TM_FWD><<<grid, THREADS, CS, st>>>(a); break;
       case TM_INV: k_col<N, TM_INV><<<grid, THREADS, CS, st>>>(a); break;
-      case TM_WIN: k_col<N, TM_WIN><<<grid, CW::THREADS, CSW, st>>>(a); break;
+      case TM_WIN: launch_win<0>(a.win_var, grid, st, a); break;
       default: k_col<N, TM_ACC><<<grid, CA::THREADS, CSA, st>>>(a); break;
     }
   }
@@ -97,20 +144,30 @@ template <int N> struct Launchers {
   static cudaError_t init(KernelSet* ks) {
     void* tf = CL::template fn<TM_FWD>();
     void* ti = CL::template fn<TM_INV>();
-    void* tw = CL::template fn<TM_WIN>();
     void* ta = CL::template fn<TM_ACC>();
     cudaError_t e;
     if ((e = smem(tf, CL::bytes(TM_FWD))) != cudaSuccess) return e;
     if ((e = smem(ti, CL::bytes(TM_INV))) != cudaSuccess) return e;
-    if ((e = smem(tw, CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = smem(ta, CL::bytes(TM_ACC))) != cudaSuccess) return e;
+    // window-pass variants
+    ks->n_win_var = CL::win(0);
+    for (int v = 0; v < ks->n_win_var; ++v) {
+      void* f = nullptr;
+      int thr = 0, tw = 0;
+      size_t by = 0;
+      CL::win(v, &f, &thr, &by, &tw);
+      if ((e = smem(f, by)) != cudaSuccess) return e;
+      if ((e = occ(&ks->occ_winv[v], f, thr, by)) != cudaSuccess) return e;
+      ks->tile_w_winv[v] = tw;
+    }
+    ks->occ_tile_win = ks->occ_winv[0];
+    ks->tile_w_win = ks->tile_w_winv[0];
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
     for (int i = 0; i < CR::NFN; ++i)
       if ((e = smem(CR::fn(i), CR::BYTES)) != cudaSuccess) return e;
     if ((e = smem(&k_adj_z<N>, LS)) != cudaSuccess) return e;
     if ((e = smem(&k_c2r_plain<N>, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile, ti, CL::THREADS, CL::bytes(TM_INV))) != cudaSuccess) return e;
-    if ((e = occ(&ks->occ_tile_win, tw, CL::threads(TM_WIN), CL::bytes(TM_WIN))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_tile_acc, ta, CL::threads(TM_ACC), CL::bytes(TM_ACC))) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_r2c, &k_r2c_z<N>, LL::THREADS, LS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_c2r, CR::fn(0), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
@@ -137,8 +194,8 @@ template <int N> struct Launchers {
     ks.N = N;
     ks.tile_threads = CL::THREADS;
     ks.tile_w = CL::T;
-    ks.tile_w_win = CL::T_WIN;
     ks.tile_w_acc = CL::T_ACC;
+    ks.n_win_var = CL::win(0);
     ks.line_threads = LL::THREADS;
     ks.line_groups = LL::NG;
     ks.c2r_lines = CR::NG;

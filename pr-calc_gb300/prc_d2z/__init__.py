@@ -34,7 +34,7 @@ from ._lib import (PRC_ARGMAX_NONE, PRC_FLAG_ARGMAX, PRC_FLAG_SIGMA_GRID, PRC_NH
 __all__ = ["Parameters", "CLParameters", "Tables", "read_parameter_file", "compute_tables",
            "Delta2Zreion", "delta2zreion", "PrcError", "PRC_ARGMAX_NONE", "PRC_NHISTORY",
            "supported_sizes", "growth", "inverse_erfc", "tau", "Float2FloatTable", "fcoll",
-           "chistory", "zvz_map", "Batch"]
+           "chistory", "zvz_map", "Batch", "win_variants"]
 
 
 @dataclass
@@ -209,6 +209,11 @@ def compute_tables(p: Parameters, cl: CLParameters) -> Tables:
     return Tables(t.DInit, t.zHigh, t.DHigh, t.pnorm, t.erfizeta, t.sigma_min, t.barrier_a, R, S, B)
 
 
+def win_variants(N: int) -> int:
+    """Window-pass variants compiled for grid side N (prc_d2z_win_variants)."""
+    return int(load().prc_d2z_win_variants(int(N)))
+
+
 def supported_sizes() -> list[int]:
     L = load()
     return [n for n in range(2, 2049) if L.prc_d2z_supported(n)]
@@ -348,6 +353,11 @@ class Delta2Zreion:
         check(L.prc_d2z_gaussian_field(self._ctx, int(seed) & 0xFFFFFFFF, a.ctypes.data, len(a),
                                        _host_ptr(res, np.float32, self.n3), 0))
         return res
+
+    def tune(self, radius_batch: int = 0, win_variant: int = 0) -> None:
+        """Radius batch (0 = keep) and window-pass variant (prc_d2z_tune)."""
+        check(load().prc_d2z_tune(self._ctx, int(radius_batch), int(win_variant)))
+        self.radius_batch, self.win_variant = int(radius_batch), int(win_variant)
 
     def set_barrier(self, barrier_b, barrier_a: float) -> None:
         """New barrier table for the same radii (prc_d2z_set_barrier)."""
@@ -500,6 +510,10 @@ class Batch:
         n = ctypes.c_int()
         check(load().prc_d2z_batch_launches(self._b, ctypes.byref(n)))
         return n.value
+
+    def tune(self, box: int, radius_batch: int = 0, win_variant: int = 0) -> None:
+        """Radius batch and window-pass variant of one box (prc_d2z_batch_tune)."""
+        check(load().prc_d2z_batch_tune(self._b, int(box), int(radius_batch), int(win_variant)))
 
     def close(self):
         if getattr(self, "_b", None) and self._b.value:

@@ -34,7 +34,8 @@ EXPORTS = [
     "prc_f2f_load", "prc_f2f_eval", "prc_f2f_free", "prc_deltac", "prc_fcoll", "prc_d2z_bubble_mfp",
     "prc_chistory", "prc_zvz", "prc_d2z_correct", "prc_d2z_batch_create", "prc_d2z_batch_forward",
     "prc_d2z_batch_launches", "prc_d2z_batch_destroy", "prc_d2z_set_barrier",
-    "prc_white_noise", "prc_d2z_gaussian_field", "prc_last_error",
+    "prc_white_noise", "prc_d2z_gaussian_field", "prc_d2z_win_variants", "prc_d2z_tune",
+    "prc_d2z_batch_tune", "prc_last_error",
 ]
 
 
@@ -137,6 +138,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_d2z_batch_launches.argtypes = [vp, P(c_int)]
     L.prc_d2z_batch_destroy.argtypes = [vp]
     L.prc_d2z_set_barrier.argtypes = [vp, vp, c_double]
+    L.prc_d2z_win_variants.argtypes = [c_int]
+    L.prc_d2z_tune.argtypes = [vp, c_int, c_int]
+    L.prc_d2z_batch_tune.argtypes = [vp, c_int, c_int, c_int]
     L.prc_white_noise.argtypes = [vp, ctypes.c_longlong, ctypes.c_uint, vp]
     L.prc_d2z_gaussian_field.argtypes = [vp, ctypes.c_uint, vp, c_int, vp, c_int]
     for name in EXPORTS:

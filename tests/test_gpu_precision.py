@@ -7,7 +7,8 @@ and the last radius; zreion within eps_z = A 1e-5 max|delta_R| + 2 ulp and the
 same argmax for every cell whose top-two margin (best vs runner-up radius, or
 vs the initial zreion = 0) exceeds eps_z; the near-barrier fraction is
 reported (about 1% at 512^3 x 64: adjacent radii of a dense log grid give
-close z) and must stay below 5%."""
+close z) and must stay below 5%; the ionisation history x_i(z) of the GPU
+zreion within 1e-4 of that of the FP64 zreion."""
 import math
 
 import numpy as np
@@ -104,4 +105,10 @@ def test_full_size_against_fp64(N, box, nr, zeta):
         dz = (z.double() - zo).abs()
         assert bool((dz[clear] <= eps[clear]).all()), float(dz[clear].max())
         assert bool((am[clear] == amo[clear]).all())
-        print(f"N={N}: near-barrier fraction {frac_near:.2e}, max |dz| on clear cells {float(dz[clear].max()):.3e}")
+        # ionisation history x_i(z) (GetHistory of each field) within 1e-4
+        _, x_gpu, _ = ctx.history(z)
+        _, x_64, _ = ctx.history(zo.float().contiguous())
+        dx = float(np.max(np.abs(x_gpu.astype(np.float64) - x_64.astype(np.float64))))
+        assert dx <= 1e-4, dx
+        print(f"N={N}: near-barrier fraction {frac_near:.2e}, max |dz| on clear cells {float(dz[clear].max()):.3e}, "
+              f"max |dx_i| {dx:.2e}")
