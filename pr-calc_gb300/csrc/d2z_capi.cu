@@ -393,7 +393,10 @@ void forward_r2c(prc_d2z_ctx* c, const float* d_delta, double divisor) {
 
 // All radius sweeps of a forward call, kernels only (no copies, events or
 // synchronisation), so that the same sequence can be captured into a graph.
-void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig) {
+// The running max lives in d_z / d_am; the last sweep writes the final values
+// to z_out / am_out (default: d_z / d_am), which may be mapped host memory.
+void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, float* z_out = nullptr,
+                    uint8_t* am_out = nullptr) {
   const int N = c->N, H = c->H;
   const long long NN = c->NN;
   for (int r0 = 0; r0 < c->nr; r0 += c->B) {
@@ -403,8 +406,11 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig) {
     sa.slots = c->slots;
     sa.slot_stride = c->slot_f2;
     sa.tw = c->tw;
+    const bool last = (r0 + nb >= c->nr);
     sa.zreion = d_z;
     sa.argmax = d_am;
+    sa.zreion_out = (last && z_out) ? z_out : d_z;
+    sa.argmax_out = d_am ? ((last && am_out) ? am_out : d_am) : nullptr;
     sa.sig_acc = sig;
     sa.nb = nb;
     sa.r0 = r0;
@@ -552,6 +558,19 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
   return PRC_OK;
 }
 
+namespace {
+// Device address of a host buffer the GPU reads and writes in place (pinned
+// and mapped into the device's address space), or null (then it is staged).
+void* mapped_view(const void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
+}
+}  // namespace
+
 int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device, float* zreion,
                     uint8_t* argmax, int out_on_device, double* sigma_grid) {
   int st;
@@ -563,11 +582,27 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
   c->launches = 0;
   c->have_timing = 0;
   // device buffers
+  // host buffers: a pinned, mapped one is read (delta) or written (the last
+  // sweep's zreion / argmax) in place over the host link; others are staged
   const float* d_delta = delta_lin;
   if (!delta_on_device) {
-    float* stage = reinterpret_cast<float*>(c->slots);  // slot 0 main region holds N^3 floats
-    PRC_CU(cudaMemcpyAsync(stage, delta_lin, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D delta");
-    d_delta = stage;
+    if (const void* v = mapped_view(delta_lin)) {
+      d_delta = static_cast<const float*>(v);
+    } else {
+      float* stage = reinterpret_cast<float*>(c->slots);  // slot 0 main region holds N^3 floats
+      PRC_CU(cudaMemcpyAsync(stage, delta_lin, sizeof(float) * n3, cudaMemcpyHostToDevice, c->st), "H2D delta");
+      d_delta = stage;
+    }
+  }
+  float* z_final = nullptr;     // mapped host output of the last sweep
+  uint8_t* am_final = nullptr;
+  if (!out_on_device) {
+    void* zv = mapped_view(zreion);
+    void* av = argmax ? mapped_view(argmax) : nullptr;
+    if (zv && (!argmax || av)) {
+      z_final = static_cast<float*>(zv);
+      am_final = static_cast<uint8_t*>(av);
+    }
   }
   float* d_z = zreion;
   uint8_t* d_am = argmax;
@@ -585,12 +620,14 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
   PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
   forward_r2c(c, d_delta, c->dinit);
   PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
-  enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr);
+  enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr, z_final, am_final);
   PRC_CU(cudaGetLastError(), "kernel launch");
   PRC_CU(cudaEventRecord(c->ev[2], c->st), "event");
   if (!out_on_device) {
-    PRC_CU(cudaMemcpyAsync(zreion, d_z, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H zreion");
-    if (argmax) PRC_CU(cudaMemcpyAsync(argmax, d_am, n3, cudaMemcpyDeviceToHost, c->st), "D2H argmax");
+    if (!z_final) {
+      PRC_CU(cudaMemcpyAsync(zreion, d_z, sizeof(float) * n3, cudaMemcpyDeviceToHost, c->st), "D2H zreion");
+      if (argmax) PRC_CU(cudaMemcpyAsync(argmax, d_am, n3, cudaMemcpyDeviceToHost, c->st), "D2H argmax");
+    }
   } else if (argmax && d_am != argmax) {
     PRC_CU(cudaMemcpyAsync(argmax, d_am, n3, cudaMemcpyDeviceToDevice, c->st), "D2D argmax");
   }

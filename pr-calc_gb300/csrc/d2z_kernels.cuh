@@ -120,8 +120,10 @@ struct SweepArgs {
   float2* slots;        // slot 0 base
   long long slot_stride;
   const float2* tw;
-  float* zreion;        // N^3
+  float* zreion;        // N^3: running max read at the start of the sweep
   uint8_t* argmax;      // N^3 or null
+  float* zreion_out;    // where the sweep writes it (may be mapped host memory)
+  uint8_t* argmax_out;  // likewise for the argmax (null when argmax is null)
   double* sig_acc;      // per-radius sum of x^2 (raw C2R units) or null
   int nb;               // radii in this sweep
   int r0;               // global index of the first radius
@@ -736,11 +738,13 @@ __global__ void __launch_bounds__(LK<N>::THREADS, LK<N>::MINB) k_c2r_z(SweepArgs
       }
     }
     if (valid) {
+      float* zo = a.zreion_out + (long long)lv * N;
+      uint8_t* ao = a.argmax_out ? a.argmax_out + (long long)lv * N : nullptr;
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int p = t + G * m;
-        reinterpret_cast<float2*>(zline)[p] = zr[m];
-        if (aline) reinterpret_cast<uint16_t*>(aline)[p] = (uint16_t)am[m];
+        reinterpret_cast<float2*>(zo)[p] = zr[m];
+        if (ao) reinterpret_cast<uint16_t*>(ao)[p] = (uint16_t)am[m];
       }
     }
   }

@@ -122,6 +122,8 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
     const long long l = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG + g;
     float* zline = a.zreion + l * N;
     uint16_t* aline = AM ? reinterpret_cast<uint16_t*>(a.argmax + l * N) : nullptr;
+    float* zout = a.zreion_out + l * N;
+    uint16_t* aout = AM ? reinterpret_cast<uint16_t*>(a.argmax_out + l * N) : nullptr;
     if (b == 0) {
       if (a.first) {
 #pragma unroll
@@ -212,8 +214,8 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int p = t + G * m;
-        reinterpret_cast<float2*>(zline)[p] = zr[m];
-        if constexpr (AM) aline[p] = (uint16_t)(am[m >> 1] >> (16 * (m & 1)));
+        reinterpret_cast<float2*>(zout)[p] = zr[m];
+        if constexpr (AM) aout[p] = (uint16_t)(am[m >> 1] >> (16 * (m & 1)));
       }
     }
     lg = lg_next;

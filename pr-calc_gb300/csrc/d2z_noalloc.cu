@@ -191,6 +191,8 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     sa.tw = tw;
     sa.zreion = d_zreion;
     sa.argmax = d_argmax;
+    sa.zreion_out = d_zreion;
+    sa.argmax_out = d_argmax;
     sa.sig_acc = nullptr;
     sa.nb = 1;
     sa.r0 = r;

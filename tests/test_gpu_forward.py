@@ -105,3 +105,27 @@ def test_history_counts_exact():
     assert np.array_equal(counts, co)
     np.testing.assert_array_equal(hist, ho)
     np.testing.assert_array_equal(hz[1:], hzo[1:])
+
+
+@pytest.mark.parametrize("want_argmax", [False, True])
+def test_pinned_host_buffers_read_and_written_in_place(want_argmax):
+    """Pinned (mapped) host buffers are read by the forward R2C and written by
+    the last sweep in place; the result is bit-identical to the device path
+    and to the staged path of pageable buffers."""
+    import torch
+    p, cl, delta, t, box_mpc = _setup(64, nscales=12)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=5) as ctx:
+        zd, ad, _ = ctx.forward(torch.from_numpy(delta).cuda(), want_argmax=want_argmax)
+        torch.cuda.synchronize()
+        hd = torch.empty(delta.shape, dtype=torch.float32, pin_memory=True)
+        hd.copy_(torch.from_numpy(delta))
+        hz = torch.full(delta.shape, -7.0, dtype=torch.float32, pin_memory=True)
+        ha = torch.zeros(delta.shape, dtype=torch.uint8, pin_memory=True) if want_argmax else None
+        for _ in range(2):  # twice: the running max must not leak between calls
+            ctx.forward(hd.numpy(), zreion=hz.numpy(), argmax=ha.numpy() if want_argmax else None,
+                        want_argmax=want_argmax)
+            assert np.array_equal(hz.numpy(), zd.cpu().numpy())
+            if want_argmax:
+                assert np.array_equal(ha.numpy(), ad.cpu().numpy())
+        zp, ap, _ = ctx.forward(delta.copy(), want_argmax=want_argmax)   # pageable: staged copies
+        assert np.array_equal(zp, zd.cpu().numpy())
