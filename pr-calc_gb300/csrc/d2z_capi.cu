@@ -206,6 +206,7 @@ struct prc_d2z_ctx {
   float* gstage = nullptr;
   uint8_t* amstage = nullptr;
   float* grf_amp = nullptr;       // field generator: amplitude by |m|^2
+  int* err = nullptr;             // set by a kernel whose copy wait ran out
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float last_ms[3] = {0, 0, 0};
   int have_timing = 0;
@@ -294,6 +295,7 @@ void free_all(prc_d2z_ctx* c) {
   cudaFree(c->gstage);
   cudaFree(c->amstage);
   cudaFree(c->grf_amp);
+  cudaFree(c->err);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->pev) cudaEventDestroy(e);
@@ -412,6 +414,7 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, floa
     sa.zreion_out = (last && z_out) ? z_out : d_z;
     sa.argmax_out = d_am ? ((last && am_out) ? am_out : d_am) : nullptr;
     sa.sig_acc = sig;
+    sa.err = c->err;
     sa.nb = nb;
     sa.r0 = r0;
     sa.first = (r0 == 0);
@@ -535,10 +538,16 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
       (st = dalloc(&c->tw, (size_t)c->N, "twiddles")) != PRC_OK ||
       (st = dalloc(&c->sig, (size_t)c->nr, "sigma accumulators")) != PRC_OK ||
       (st = dalloc(&c->dB, (size_t)c->nr, "barrier gradient")) != PRC_OK ||
-      (st = dalloc(&c->counts, (size_t)kNHistory, "history counts")) != PRC_OK) {
+      (st = dalloc(&c->counts, (size_t)kNHistory, "history counts")) != PRC_OK ||
+      (st = dalloc(&c->err, (size_t)1, "error flag")) != PRC_OK) {
     free_all(c);
     delete c;
     return st;
+  }
+  if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) {
+    free_all(c);
+    delete c;
+    return cuda_fail(e, "prc_d2z_create: error flag");
   }
   (void)n3l;
   // twiddles e^{+2 pi i k/N}, FP64 on the host
@@ -559,6 +568,17 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
 }
 
 namespace {
+// Reads and clears the context's kernel error flag (after a synchronisation).
+int check_kernel_flag(prc_d2z_ctx* c, const char* who) {
+  int h = 0;
+  PRC_CU(cudaMemcpy(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+  if (h) {
+    cudaMemset(c->err, 0, sizeof(int));
+    return prc_fail(PRC_ERR_CUDA, "%s: a staging copy did not complete within the wait limit", who);
+  }
+  return PRC_OK;
+}
+
 // Device address of a host buffer the GPU reads and writes in place (pinned
 // and mapped into the device's address space), or null (then it is staged).
 void* mapped_view(const void* host) {
@@ -637,6 +657,7 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
     PRC_CU(cudaMemcpyAsync(sig.data(), c->sig, sizeof(double) * c->nr, cudaMemcpyDeviceToHost, c->st), "D2H sigma");
   }
   PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_forward");
+  if ((st = check_kernel_flag(c, "prc_d2z_forward")) != PRC_OK) return st;
   prof_collect(c);
   float t0, t1;
   PRC_CU(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]), "event time");
@@ -1048,13 +1069,15 @@ int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* co
   if (!b || !delta || !zreion) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null argument");
   for (int i = 0; i < b->n; ++i)
     if (!delta[i] || !zreion[i]) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null pointer for box %d", i);
-  int cur = -1;
+  int cur = -1, st;
   PRC_CU(cudaGetDevice(&cur), "cudaGetDevice");
   if (cur != b->dev) PRC_CU(cudaSetDevice(b->dev), "cudaSetDevice");
   if (!use_graph) {
     batch_enqueue(b, delta, zreion, argmax);
     PRC_CU(cudaGetLastError(), "prc_d2z_batch_forward");
     PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
+    for (auto* c : b->ctx)
+      if ((st = check_kernel_flag(c, "prc_d2z_batch_forward")) != PRC_OK) return st;
     return PRC_OK;
   }
   std::vector<const void*> key;
@@ -1079,6 +1102,8 @@ int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* co
   }
   PRC_CU(cudaGraphLaunch(b->exec, b->origin), "graph launch");
   PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
+  for (auto* c : b->ctx)
+    if ((st = check_kernel_flag(c, "prc_d2z_batch_forward")) != PRC_OK) return st;
   return PRC_OK;
 }
 

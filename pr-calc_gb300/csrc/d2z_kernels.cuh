@@ -125,6 +125,7 @@ struct SweepArgs {
   float* zreion_out;    // where the sweep writes it (may be mapped host memory)
   uint8_t* argmax_out;  // likewise for the argmax (null when argmax is null)
   double* sig_acc;      // per-radius sum of x^2 (raw C2R units) or null
+  int* err;             // set to 1 when a copy wait ran out (null: not reported)
   int nb;               // radii in this sweep
   int r0;               // global index of the first radius
   int first;            // first sweep: zreion/argmax not read

@@ -52,15 +52,46 @@ template <int N> struct PK {
   static constexpr int smem_f2 = N + TW + NG * gsize + 2 * STG + 2 * NG;
 };
 
-// 16-byte asynchronous global -> shared copy (L2 only).
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+// TMA bulk copies (cp.async.bulk) completing on an mbarrier.
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(s), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// one arrival that also announces `bytes` of transactions, then the copy
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, unsigned bytes, uint64_t* bar) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+               ::"r"(d), "l"(gmem_src), "r"(bytes), "r"(b)
+               : "memory");
+}
+// waits for phase `parity` of the barrier; false after `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int limit) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  for (int i = 0; i < limit; ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(b), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+constexpr int kWaitPolls = 1 << 22;  // each poll may suspend; far beyond any copy
 
 // Steps (line group s, radius b) run in order; the input of the next step is
-// copied into the other staging buffer with cp.async while the current one is
-// transformed (the NG lines of a step are one contiguous block of the slot).
+// copied into the other staging buffer while the current one is transformed:
+// the NG lines of a step are one contiguous block of the slot, fetched by one
+// TMA bulk copy (cp.async.bulk) issued by thread 0 and completing on that
+// buffer's mbarrier; the NG Nyquist values come with 8-byte cp.async.  A wait
+// that runs out of polls stops the whole CTA and sets *a.err.
 // AM: argmax wanted (a.argmax != null); its bytes are packed four to a register.
 // SIG: per-radius sums of x^2 wanted (a.sig_acc != null).
 template <int N, bool AM, bool SIG>
@@ -90,18 +121,20 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   const int nb = a.nb;
   const int total = nsteps_l > 0 ? nsteps_l * nb : 0;
 
-  // copies of step (line group lg of this CTA, radius b) into staging buffer buf
+  __shared__ __align__(8) uint64_t s_bar[2];
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+
+  // copies of step (line group lg of this CTA, radius b) into staging buffer bi
   auto issue = [&](int lg, int b, int bi) {
     if (lg < nsteps_l) {
       const long long l0 = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG;
       const float2* slot = a.slots + (long long)b * a.slot_stride;
-      const char* src = reinterpret_cast<const char*>(slot + l0 * H);
-      char* dst = reinterpret_cast<char*>(stage + bi * STG);
-#pragma unroll
-      for (int q = 0; q < (STG * 8) / (16 * KK::THREADS); ++q) {
-        const int off = (q * KK::THREADS + threadIdx.x) * 16;
-        cp_async16(dst + off, src + off);
-      }
+      if (threadIdx.x == 0) bulk_load(stage + bi * STG, slot + l0 * H, STG * 8, &s_bar[bi]);
       if (t == 0) {
         const long long l = l0 + g;
         const int ix = (int)(l / N), iy = (int)(l - (l / N) * N);
@@ -142,8 +175,14 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
         }
       }
     }
+    // step i uses buffer bi for the (i >> 1)-th time: barrier phase (i >> 1) & 1
+    const bool late = !mbar_wait(&s_bar[bi], (unsigned)((i >> 1) & 1), kWaitPolls);
     cp_async_wait<0>();
-    __syncthreads();  // step i staged for everyone; everyone is done reading buffer (i+1) & 1
+    // step i staged for everyone; everyone is done reading buffer (i+1) & 1
+    if (__syncthreads_or(late)) {
+      if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+      break;
+    }
     issue(lg_next, nb_next, bi ^ 1);
     const float2* src = stage + bi * STG + g * H;
     float2 v[E];
