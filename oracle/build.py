@@ -3,7 +3,7 @@
 Compiles oracle/d2z_cells.c into oracle/_build/liborc_cells.so with gcc,
 OpenMP and -ffp-contract=off (the reference's float expressions round per
 operation).  The reference itself is not built: it needs MPI, FFTW 3.3.3 and
-GSL, none of which are installed on either machine, so there is no
+GSL, none of which are installed where this code is built and run, so there is no
 oracle/_ref.
 """
 import os

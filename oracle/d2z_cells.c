@@ -3,10 +3,11 @@
  * per-cell and per-mode loops of pr-calc's delta2zreion step, with the
  * reference's float/double conversions kept operation by operation.  Only the
  * tests, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
- * load this library, and only as the checker; the product never does.
+ * load this library, and only to check results against it; the product never
+ * does.
  *
  * Parity is unpinned: the reference (c++/src) needs MPI, FFTW 3.3.3 and GSL,
- * none of which exist on either machine, and it ships no test vectors.  These
+ * none of which are installed where this code is built and run, and it ships no test vectors.  These
  * loops follow its source line by line instead:
  *   orc_window_faithful  delta2zreion_d2z.C:41-43,58-89  (float kx, ky, kz,
  *                        sqrtf of the float sum, W = 3.*(sinf-x*cosf)/pow(x,3)

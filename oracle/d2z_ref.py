@@ -2,11 +2,11 @@
 
 A restatement of pr-calc's ``delta2zreion`` chain (c++/src) in numpy/scipy,
 used only by ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline / reference arm, and only as the checker.  The product never imports
-it.
+baseline / reference arm, and only to check results against it.  The product
+never imports it.
 
-Parity is unpinned: the reference needs MPI, FFTW 3.3.3 and GSL (absent here
-and on the GPU machine) and ships no golden vectors or tests for this path, so
+Parity is unpinned: the reference needs MPI, FFTW 3.3.3 and GSL (not installed
+where this code is built and run) and ships no golden vectors or tests for this path, so
 these functions follow its source, each citing the lines it restates:
 
   read_parameter_file   io_d2z.C:16-162
