@@ -511,7 +511,9 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
   c->st = (cudaStream_t)d->stream;
   c->ks = ks;
   c->ksl = *ks;
-  int B = d->radius_batch ? d->radius_batch : 8;
+  // default radii per sweep: 16 (measured fastest up to 512^3: fewer re-reads
+  // of the spectrum and of zreion), 8 at 1024^3 where one slot is 4.3 GB
+  int B = d->radius_batch ? d->radius_batch : (d->N >= 1024 ? 8 : 16);
   if (B > c->nr) B = c->nr;
   c->B = B;
   c->slots_b = B;
