@@ -51,9 +51,10 @@ template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<1
 template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
-// N = 1024: 64 lanes x 8 columns in every pass.  (Plain passes on 32 lanes x
-// 16 columns with 32 elements a lane -- 128-byte rows, but one exchange buffer
-// and no register prefetch -- measured 1% slower over the whole step.)
+// N = 1024: 64 lanes x 8 columns in every pass.  (Measured no faster: plain
+// passes on 32 lanes x 16 columns with 32 elements a lane, and on 64 lanes x 16
+// columns in 1024-thread CTAs of 64 registers -- both 128-byte rows, one
+// exchange buffer, no register prefetch -- 1-2% slower over the whole step.)
 template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
 template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
@@ -121,7 +122,8 @@ template <> struct WinVar<512, 2> { static constexpr bool on = true; static cons
 // accumulate mode uses variant 0 of the window pass when the plain plan holds
 // more than 16 elements a lane (its accumulator would not fit beside them).
 template <int N, int MODE> struct ColUsesWin {
-  static constexpr bool v = MODE == TM_WIN || (MODE == TM_ACC && CCfg<N>::P::E > 16);
+  static constexpr bool v =
+      MODE == TM_WIN || (MODE == TM_ACC && (CCfg<N>::P::E > 16 || CCfg<N>::T * (N / CCfg<N>::P::E) > 512));
 };
 template <int N, int MODE, int V> struct ColK {
   static constexpr int VV = MODE == TM_WIN ? V : 0;
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     }
   };
 
-  if constexpr ((MODE == TM_FWD || MODE == TM_INV) && E <= 16) {
+  if constexpr ((MODE == TM_FWD || MODE == TM_INV) && E <= 16 && KK::THREADS <= 512) {
     float2 v[E], nx[E];
     int ti = blockIdx.x;
     if (ti < tiles) {
@@ -249,8 +251,8 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       for (int m = 0; m < E; ++m) v[m] = nx[m];
     }
   } else if constexpr (MODE == TM_FWD || MODE == TM_INV) {
-    // 32 elements a lane: no room for a prefetch; 32 independent loads per
-    // lane keep enough bytes in flight on their own
+    // 32 elements a lane, or 1024-thread CTAs with 64 registers: no room for a
+    // prefetch; the independent loads of every lane keep enough bytes in flight
     for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
       float2 v[E];
