@@ -15,63 +15,11 @@ import numpy as np
 import pytest
 
 import prc_d2z
+from fp64_chain import chain as _fp64_chain
 from prc_d2z import fields
 
 pytestmark = pytest.mark.gpu
 H_ = 0.68
-
-
-def _kmag(N, box_mpc, device):
-    import torch
-    f = torch.fft.fftfreq(N, d=1.0 / N, device=device, dtype=torch.float64)
-    fz = torch.arange(N // 2 + 1, device=device, dtype=torch.float64)
-    dk = 2.0 * math.pi / box_mpc
-    k2 = (f[:, None, None] ** 2 + f[None, :, None] ** 2 + fz[None, None, :] ** 2) * dk * dk
-    return torch.sqrt(k2)
-
-
-def _tophat64(x):
-    import torch
-    small = x < 1e-2
-    xs = torch.where(small, torch.ones_like(x), x)
-    w = 3.0 * (torch.sin(xs) - xs * torch.cos(xs)) / xs ** 3
-    x2 = x * x
-    ws = 1.0 - x2 / 10.0 + x2 * x2 / 280.0
-    return torch.where(small, ws, w)
-
-
-def _fp64_chain(delta, box_mpc, R, A, B, dinit, radii_check):
-    """zreion / argmax / top-two margin / max|delta_R| and delta_R of the
-    radii in radii_check, all in FP64 on the GPU."""
-    import torch
-    N = delta.shape[0]
-    dev = delta.device
-    spec = torch.fft.rfftn(delta.double() / dinit)
-    kmag = _kmag(N, box_mpc, dev)
-    best = torch.full(delta.shape, -math.inf, dtype=torch.float64, device=dev)
-    second = best.clone()
-    am = torch.full(delta.shape, 255, dtype=torch.uint8, device=dev)
-    dmax = 0.0
-    keep = {}
-    for r in range(len(R)):
-        W = _tophat64(kmag * R[r])
-        W[0, 0, 0] = 0.0
-        dR = torch.fft.irfftn(spec * W, s=(N, N, N))
-        del W
-        dmax = max(dmax, float(dR.abs().max()))
-        if r in radii_check:
-            keep[r] = dR.clone()
-        z = A * (dR + B[r]) - 1.0
-        del dR
-        gt = z > best
-        second = torch.where(gt, best, torch.where(z > second, z, second))
-        best = torch.where(gt, z, best)
-        am[gt] = r
-        del z, gt
-    zo = torch.where(best > 0, best, torch.zeros_like(best))
-    am = torch.where(best > 0, am, torch.full_like(am, 255))
-    gap = torch.minimum(best - second, best.abs())
-    return zo, am, gap, dmax, keep
 
 
 @pytest.mark.parametrize("N,box,nr,zeta", [(512, 600.0, 64, 80.5404), (1024, 1200.0, 96, 73.1587)])
