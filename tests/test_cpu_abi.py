@@ -89,3 +89,14 @@ def test_python_binding_raises_loudly_without_library(tmp_path):
             _lib.load(str(tmp_path / "nope.so"))
         finally:
             _lib._lib = _lib._lib_saved
+
+
+@pytest.mark.parametrize("nscales", [1, 255])
+def test_tables_reject_radius_counts_the_reference_does_not_check(nscales):
+    # Nscales = 1 makes the reference's radius spacing a division by zero
+    # (delta2zreion_d2z.C:38); more than 254 radii do not fit the argmax byte
+    p = prc_d2z.Parameters(N=32, Nscales=nscales, BoxSize=100.0)
+    cl = prc_d2z.CLParameters(Rmax=60.0, zeta=80.5, M_min=1e9 / 0.68)
+    with pytest.raises(_lib.PrcError) as e:
+        prc_d2z.compute_tables(p, cl)
+    assert e.value.code == _lib.PRC_ERR_INVALID
