@@ -147,6 +147,17 @@ int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_devic
                     float* zreion, uint8_t* argmax, int out_on_device,
                     double* sigma_grid);
 
+/* prc_d2z_forward over n boxes of this context's shape, all from host
+ * buffers (delta[i] -> zreion[i], argmax[i]; argmax may be null): a stream of
+ * realisations, as a driver that loops main_d2z.C:57-71 over input files
+ * would run it.  Box i+1's input is copied in and box i-1's outputs copied
+ * out by the copy engines while box i's kernels run (pinned buffers; pageable
+ * ones are correct but serialise).  Results equal n calls of
+ * prc_d2z_forward.  Returns when every output is on the host.  No
+ * counterpart in the reference, which processes one box per run. */
+int prc_d2z_forward_many(prc_d2z_ctx* ctx, int n, const float* const* delta,
+                         float* const* zreion, uint8_t* const* argmax);
+
 /* The smoothed field of one radius, delta_R = C2R(W_R * R2C(delta_lin/D_init))/N^3
  * (delta2zreion_d2z.C:57-93), written to delta_r (N^3).  A diagnostic beside
  * prc_d2z_forward, which never materialises delta_R. */

@@ -207,6 +207,17 @@ struct prc_d2z_ctx {
   uint8_t* amstage = nullptr;
   float* grf_amp = nullptr;       // field generator: amplitude by |m|^2
   int* err = nullptr;             // set by a kernel whose copy wait ran out
+  // prc_d2z_forward_many: two device copies of a box's input and outputs and
+  // two copy streams (in, out), so that the copies of neighbouring boxes run
+  // on the copy engines while this box's kernels run
+  float* m_delta[2] = {nullptr, nullptr};
+  float* m_z[2] = {nullptr, nullptr};
+  uint8_t* m_am[2] = {nullptr, nullptr};
+  cudaStream_t m_copy[2] = {nullptr, nullptr};
+  cudaEvent_t m_in[2] = {nullptr, nullptr};    // input copied
+  cudaEvent_t m_read[2] = {nullptr, nullptr};  // input consumed (forward R2C done)
+  cudaEvent_t m_done[2] = {nullptr, nullptr};  // outputs final
+  cudaEvent_t m_out[2] = {nullptr, nullptr};   // outputs copied out
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float last_ms[3] = {0, 0, 0};
   int have_timing = 0;
@@ -298,6 +309,14 @@ void free_all(prc_d2z_ctx* c) {
   cudaFree(c->err);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(c->m_delta[k]);
+    cudaFree(c->m_z[k]);
+    cudaFree(c->m_am[k]);
+    if (c->m_copy[k]) cudaStreamDestroy(c->m_copy[k]);
+    for (cudaEvent_t e : {c->m_in[k], c->m_read[k], c->m_done[k], c->m_out[k]})
+      if (e) cudaEventDestroy(e);
+  }
   for (auto& e : c->pev) cudaEventDestroy(e);
   c->pev.clear();
 }
@@ -581,6 +600,20 @@ int check_kernel_flag(prc_d2z_ctx* c, const char* who) {
   return PRC_OK;
 }
 
+// One cudaMemcpyAsync per piece of at most 256 MiB (a single 4 GiB host to
+// device copy from pinned memory was measured at 28 GB/s, its 512 MiB pieces
+// at the link's 207 GB/s).
+cudaError_t copy_chunked(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  constexpr size_t kPiece = size_t(256) << 20;
+  for (size_t off = 0; off < bytes; off += kPiece) {
+    const size_t nb = (bytes - off < kPiece) ? bytes - off : kPiece;
+    const cudaError_t e = cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, nb,
+                                          kind, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Device address of a host buffer the GPU reads and writes in place (pinned
 // and mapped into the device's address space), or null (then it is staged).
 void* mapped_view(const void* host) {
@@ -673,6 +706,87 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
     const double n3d = (double)n3;
     for (int r = 0; r < c->nr; ++r) sigma_grid[r] = sqrt(sig[r] / (n3d * n3d * n3d));
   }
+  return PRC_OK;
+}
+
+// Many boxes of this context's shape from host buffers, pipelined over two
+// device copies of the input and outputs: box i's kernels run on the
+// context's stream while box i+1's delta_lin is copied in on one copy stream
+// and box i-1's zreion (argmax) copied out on the other.  Events order each
+// buffer's reuse: box i+1's input copy waits for box i's R2C (hence for box
+// i-1's, which used the same buffer), and box i+2's kernels wait for box i's
+// output copy.  Pinned host buffers overlap;
+// pageable ones are correct but serialise (their copies block the host).
+int prc_d2z_forward_many(prc_d2z_ctx* c, int n, const float* const* delta, float* const* zreion,
+                         uint8_t* const* argmax) {
+  int st;
+  if ((st = check_ctx(c)) != PRC_OK) return st;
+  if (n < 0 || (n > 0 && (!delta || !zreion)))
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_forward_many: bad box count or null pointer array");
+  for (int i = 0; i < n; ++i)
+    if (!delta[i] || !zreion[i] || (argmax && !argmax[i]))
+      return prc_fail(PRC_ERR_INVALID, "prc_d2z_forward_many: null pointer for box %d", i);
+  if (n == 0) return PRC_OK;
+  if ((st = set_device(c)) != PRC_OK) return st;
+  const long long n3 = c->NN * c->N;
+  const bool want_am = argmax != nullptr;
+  for (int k = 0; k < 2; ++k) {
+    if (!c->m_delta[k] && (st = dalloc(&c->m_delta[k], (size_t)n3, "pipelined input")) != PRC_OK) return st;
+    if (!c->m_z[k] && (st = dalloc(&c->m_z[k], (size_t)n3, "pipelined zreion")) != PRC_OK) return st;
+    if (want_am && !c->m_am[k] && (st = dalloc(&c->m_am[k], (size_t)n3, "pipelined argmax")) != PRC_OK)
+      return st;
+    if (!c->m_copy[k]) PRC_CU(cudaStreamCreateWithFlags(&c->m_copy[k], cudaStreamNonBlocking), "copy stream");
+    for (cudaEvent_t* e : {&c->m_in[k], &c->m_read[k], &c->m_done[k], &c->m_out[k]})
+      if (!*e) PRC_CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "pipeline event");
+  }
+  cudaStream_t cin = c->m_copy[0], cout = c->m_copy[1];
+  c->launches = 0;
+  c->have_timing = 0;
+  // the first input copies may not overtake work already queued on the stream
+  PRC_CU(cudaEventRecord(c->m_read[0], c->st), "event");
+  PRC_CU(cudaEventRecord(c->m_read[1], c->st), "event");
+  PRC_CU(cudaEventRecord(c->m_out[0], c->st), "event");
+  PRC_CU(cudaEventRecord(c->m_out[1], c->st), "event");
+  for (int i = 0; i < n; ++i) {
+    const int k = i & 1;
+    // the first box has nothing to overlap its input copy with: a mapped
+    // input is read in place by its R2C instead; likewise the last box's
+    // final sweep writes mapped outputs in place
+    const float* d_in = (i == 0) ? static_cast<const float*>(mapped_view(delta[0])) : nullptr;
+    float* z_fin = nullptr;
+    uint8_t* am_fin = nullptr;
+    if (i == n - 1) {
+      z_fin = static_cast<float*>(mapped_view(zreion[i]));
+      am_fin = want_am ? static_cast<uint8_t*>(mapped_view(argmax[i])) : nullptr;
+      if (want_am && !am_fin) z_fin = nullptr;
+    }
+    if (!d_in) {
+      // after the previous box's R2C: it may be reading its input over the
+      // host link, and the box before it (same buffer) is past its R2C too
+      PRC_CU(cudaStreamWaitEvent(cin, c->m_read[i == 0 ? k : (i - 1) & 1], 0), "wait");
+      PRC_CU(copy_chunked(c->m_delta[k], delta[i], sizeof(float) * n3, cudaMemcpyHostToDevice, cin), "H2D delta");
+      PRC_CU(cudaEventRecord(c->m_in[k], cin), "event");
+      PRC_CU(cudaStreamWaitEvent(c->st, c->m_in[k], 0), "wait");
+      d_in = c->m_delta[k];
+    }
+    PRC_CU(cudaStreamWaitEvent(c->st, c->m_out[k], 0), "wait");
+    forward_r2c(c, d_in, c->dinit);
+    PRC_CU(cudaEventRecord(c->m_read[k], c->st), "event");
+    enqueue_sweeps(c, c->m_z[k], want_am ? c->m_am[k] : nullptr, nullptr, z_fin, am_fin);
+    PRC_CU(cudaGetLastError(), "kernel launch");
+    PRC_CU(cudaEventRecord(c->m_done[k], c->st), "event");
+    if (!z_fin) {
+      PRC_CU(cudaStreamWaitEvent(cout, c->m_done[k], 0), "wait");
+      PRC_CU(copy_chunked(zreion[i], c->m_z[k], sizeof(float) * n3, cudaMemcpyDeviceToHost, cout), "D2H zreion");
+      if (want_am)
+        PRC_CU(copy_chunked(argmax[i], c->m_am[k], (size_t)n3, cudaMemcpyDeviceToHost, cout), "D2H argmax");
+      PRC_CU(cudaEventRecord(c->m_out[k], cout), "event");
+    }
+  }
+  PRC_CU(cudaStreamSynchronize(cout), "prc_d2z_forward_many");
+  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_forward_many");
+  if ((st = check_kernel_flag(c, "prc_d2z_forward_many")) != PRC_OK) return st;
+  prof_collect(c);
   return PRC_OK;
 }
 
@@ -1167,6 +1281,8 @@ int prc_d2z_destroy(prc_d2z_ctx* c) {
   if (!c) return PRC_OK;
   set_device(c);
   if (c->st) cudaStreamSynchronize(c->st);
+  for (cudaStream_t s : c->m_copy)
+    if (s) cudaStreamSynchronize(s);
   free_all(c);
   c->ks = nullptr;
   delete c;

@@ -324,6 +324,21 @@ class Delta2Zreion:
             check(L.prc_d2z_forward(self._ctx, dp, 0, zp, ap, 0, sig_p))
         return zreion, argmax, sig
 
+    def forward_many(self, deltas, zreions, argmaxes=None):
+        """prc_d2z_forward_many: boxes deltas[i] -> zreions[i] (argmaxes[i]), all
+        contiguous host numpy arrays of N^3 (pinned ones overlap the copies with
+        the kernels of the neighbouring boxes).  Returns zreions."""
+        n = len(deltas)
+        if len(zreions) != n or (argmaxes is not None and len(argmaxes) != n):
+            raise ValueError("deltas, zreions (and argmaxes) must have the same length")
+        dp = (ctypes.c_void_p * n)(*[_host_ptr(d, np.float32, self.n3).value for d in deltas])
+        zp = (ctypes.c_void_p * n)(*[_host_ptr(z, np.float32, self.n3).value for z in zreions])
+        ap = None
+        if argmaxes is not None:
+            ap = (ctypes.c_void_p * n)(*[_host_ptr(a, np.uint8, self.n3).value for a in argmaxes])
+        check(load().prc_d2z_forward_many(self._ctx, n, dp, zp, ap))
+        return zreions
+
     def smooth(self, delta_lin, radius: int):
         """delta_R of one radius (diagnostic; host or device like forward)."""
         L = load()

@@ -28,7 +28,8 @@ PRC_NKINDS = len(KINDS)
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
     "prc_compute_tables", "prc_growth", "prc_sigma2", "prc_inverse_erfc", "prc_tau",
-    "prc_d2z_supported", "prc_d2z_create", "prc_d2z_forward", "prc_d2z_smooth", "prc_d2z_history",
+    "prc_d2z_supported", "prc_d2z_create", "prc_d2z_forward", "prc_d2z_forward_many", "prc_d2z_smooth",
+    "prc_d2z_history",
     "prc_d2z_backward", "prc_d2z_last_timing", "prc_d2z_last_launches", "prc_d2z_profile",
     "prc_d2z_profile_read", "prc_d2z_destroy", "prc_d2z_forward_static",
     "prc_f2f_load", "prc_f2f_eval", "prc_f2f_free", "prc_deltac", "prc_fcoll", "prc_d2z_bubble_mfp",
@@ -111,6 +112,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_d2z_supported.argtypes = [c_int]
     L.prc_d2z_create.argtypes = [P(prc_d2z_desc), P(vp)]
     L.prc_d2z_forward.argtypes = [vp, vp, c_int, vp, vp, c_int, vp]
+    L.prc_d2z_forward_many.argtypes = [vp, c_int, vp, vp, vp]
     L.prc_d2z_history.argtypes = [vp, vp, c_int, vp, vp, vp]
     L.prc_d2z_smooth.argtypes = [vp, vp, c_int, c_int, vp, c_int]
     L.prc_d2z_backward.argtypes = [vp, vp, vp, c_int, vp, c_int, vp]

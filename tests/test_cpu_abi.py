@@ -75,6 +75,7 @@ def test_null_arguments_are_errors_not_crashes():
     L = _lib.load()
     assert L.prc_d2z_create(None, None) == _lib.PRC_ERR_INVALID
     assert L.prc_d2z_forward(None, None, 0, None, None, 0, None) == _lib.PRC_ERR_INVALID
+    assert L.prc_d2z_forward_many(None, 1, None, None, None) == _lib.PRC_ERR_INVALID
     assert L.prc_d2z_history(None, None, 0, None, None, None) == _lib.PRC_ERR_INVALID
     assert L.prc_d2z_backward(None, None, None, 0, None, 0, None) == _lib.PRC_ERR_INVALID
     assert L.prc_d2z_destroy(None) == _lib.PRC_OK

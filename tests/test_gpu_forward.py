@@ -129,3 +129,37 @@ def test_pinned_host_buffers_read_and_written_in_place(want_argmax):
                 assert np.array_equal(ha.numpy(), ad.cpu().numpy())
         zp, ap, _ = ctx.forward(delta.copy(), want_argmax=want_argmax)   # pageable: staged copies
         assert np.array_equal(zp, zd.cpu().numpy())
+
+
+@pytest.mark.parametrize("want_argmax,pinned", [(False, True), (True, True), (True, False)])
+def test_forward_many_equals_single_calls(want_argmax, pinned):
+    """prc_d2z_forward_many over five boxes (two device buffer sets reused
+    alternately, copies overlapping the neighbouring boxes' kernels) gives
+    each box's single-call result bit for bit."""
+    import torch
+    N, n = 64, 5
+    p, cl, _, t, box_mpc = _setup(N, nscales=12)
+    deltas = [fields.gaussian_field(N, p.BoxSize, seed=100 + i) for i in range(n)]
+
+    def host(shape, dtype, fill=0):
+        if pinned:
+            return torch.full(shape, fill, dtype=dtype, pin_memory=True).numpy()
+        return np.full(shape, fill, dtype=torch.empty(0, dtype=dtype).numpy().dtype)
+
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=5) as ctx:
+        ref = [ctx.forward(d.copy(), want_argmax=want_argmax) for d in deltas]
+        hd = [host(d.shape, torch.float32) for d in deltas]
+        for h, d in zip(hd, deltas):
+            h[...] = d
+        hz = [host(deltas[0].shape, torch.float32, -7.0) for _ in range(n)]
+        ha = [host(deltas[0].shape, torch.uint8, 0) for _ in range(n)] if want_argmax else None
+        for _ in range(2):  # twice: buffers and events are reused across calls
+            ctx.forward_many(hd, hz, ha)
+            for i in range(n):
+                assert np.array_equal(hz[i], ref[i][0]), i
+                if want_argmax:
+                    assert np.array_equal(ha[i], ref[i][1]), i
+        # a single box, and an empty list
+        ctx.forward_many(hd[:1], hz[:1], ha[:1] if want_argmax else None)
+        assert np.array_equal(hz[0], ref[0][0])
+        ctx.forward_many([], [], [] if want_argmax else None)
