@@ -27,7 +27,7 @@ def test_every_variant_matches_default(N):
     z0, a0, _ = ctx.forward(d)
     A = ctx.tables.barrier_a
     for v in range(nv):
-        for B in (4, 16):
+        for B in (4, 16, 32):
             ctx.tune(B, v)
             z, a, _ = ctx.forward(d)
             # a different radix plan only changes float rounding of delta_R
@@ -36,7 +36,7 @@ def test_every_variant_matches_default(N):
     with pytest.raises(prc_d2z.PrcError):
         ctx.tune(0, nv)
     with pytest.raises(prc_d2z.PrcError):
-        ctx.tune(17, 0)
+        ctx.tune(33, 0)   # more radii per sweep than the kernels' parameter arrays hold
     ctx.close()
 
 

@@ -85,10 +85,10 @@ def test_device_and_host_paths_agree():
     assert np.array_equal(ah, ad.cpu().numpy())
 
 
-@pytest.mark.parametrize("B", [1, 3, 5, 16])
+@pytest.mark.parametrize("B", [1, 3, 5, 16, 24, 32])
 def test_radius_batch_invariance(B):
     """The result does not depend on how radii are grouped into sweeps."""
-    p, cl, delta, t, box_mpc = _setup(32, nscales=16)
+    p, cl, delta, t, box_mpc = _setup(32, nscales=40)
     with prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=1) as c1:
         z1, a1, _ = c1.forward(delta)
     with prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=B) as cb:
