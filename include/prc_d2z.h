@@ -100,7 +100,7 @@ typedef struct {
   const double* barrier_b;        /* n_radii barrier offsets B_r (NaN: radius never wins) */
   double        barrier_a;        /* A in z = A*(delta_R + B_r) - 1             */
   double        growth_init;      /* D(zInit); delta_lin is divided by it (main_d2z.C:59) */
-  int           radius_batch;     /* radii per sweep; 0 = 16 (8 for N >= 1024)  */
+  int           radius_batch;     /* radii per sweep, <= 32; 0 = 16 (8 for N >= 1024) */
   int           flags;            /* PRC_FLAG_*                                 */
   void*         stream;           /* cudaStream_t; NULL = default stream        */
 } prc_d2z_desc;
@@ -153,7 +153,9 @@ int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_devic
  * would run it.  Box i+1's input is copied in and box i-1's outputs copied
  * out by the copy engines while box i's kernels run (pinned buffers; pageable
  * ones are correct but serialise).  Results equal n calls of
- * prc_d2z_forward.  Returns when every output is on the host.  No
+ * prc_d2z_forward.  Output buffers of different boxes must not overlap unless
+ * they are the same buffer (then the later box's result is what remains).
+ * Returns when every output is on the host.  No
  * counterpart in the reference, which processes one box per run. */
 int prc_d2z_forward_many(prc_d2z_ctx* ctx, int n, const float* const* delta,
                          float* const* zreion, uint8_t* const* argmax);

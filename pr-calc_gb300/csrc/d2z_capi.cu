@@ -755,7 +755,10 @@ int prc_d2z_forward_many(prc_d2z_ctx* c, int n, const float* const* delta, float
     const float* d_in = (i == 0) ? static_cast<const float*>(mapped_view(delta[0])) : nullptr;
     float* z_fin = nullptr;
     uint8_t* am_fin = nullptr;
-    if (i == n - 1) {
+    // (not when the previous box copies into the same buffer: that copy is
+    // ordered on the output stream only)
+    const bool reused = i > 0 && (zreion[i] == zreion[i - 1] || (want_am && argmax[i] == argmax[i - 1]));
+    if (i == n - 1 && !reused) {
       z_fin = static_cast<float*>(mapped_view(zreion[i]));
       am_fin = want_am ? static_cast<uint8_t*>(mapped_view(argmax[i])) : nullptr;
       if (want_am && !am_fin) z_fin = nullptr;

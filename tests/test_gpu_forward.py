@@ -159,6 +159,11 @@ def test_forward_many_equals_single_calls(want_argmax, pinned):
                 assert np.array_equal(hz[i], ref[i][0]), i
                 if want_argmax:
                     assert np.array_equal(ha[i], ref[i][1]), i
+        # one output buffer for every box: the last box's result remains
+        ctx.forward_many(hd, [hz[0]] * n, [ha[0]] * n if want_argmax else None)
+        assert np.array_equal(hz[0], ref[-1][0])
+        if want_argmax:
+            assert np.array_equal(ha[0], ref[-1][1])
         # a single box, and an empty list
         ctx.forward_many(hd[:1], hz[:1], ha[:1] if want_argmax else None)
         assert np.array_equal(hz[0], ref[0][0])
