@@ -280,6 +280,18 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     single_s = max_over_ranks(time.perf_counter() - t0, device=dev)
     e2e_single = world * N ** 3 * NR * args.steps / single_s
+    # the copy engines' rate on this machine, for reading the pipelined number
+    scratch = torch.empty_like(delta)
+    copy_gbs = {}
+    for kind, dst, src in (("h2d", scratch, h_delta), ("d2h", h_z[1], scratch)):
+        dst.copy_(src, non_blocking=True)
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record()
+        dst.copy_(src, non_blocking=True)
+        c1.record()
+        c1.synchronize()
+        copy_gbs[kind] = 4 * N ** 3 / (c0.elapsed_time(c1) * 1e6)
+    del scratch
     ctx.forward_many([hd, hd], hz)
     barrier()
     torch.cuda.synchronize()
@@ -328,7 +340,7 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * N ** 3, "d2h_bytes_per_step": 4 * N ** 3,
                 "api": "prc_d2z_forward_many (K boxes, pinned host buffers, copies overlapped)",
-                "single_call_value": e2e_single},
+                "single_call_value": e2e_single, "copy_engine_gbs": copy_gbs},
         "gpu_launches": launches,
         "roofline": rl,
         "canonical_3pass_gbs": canon / (ms_step * 1e-3) / 1e9,

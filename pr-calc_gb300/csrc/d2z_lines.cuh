@@ -26,24 +26,36 @@
 
 namespace prc {
 
+// Plan of the half-length line transform; THREADS / MINB: CTA size and
+// resident CTAs per SM.  Smaller CTAs wait at fewer-warp barriers and drift
+// out of phase with one another: 128-thread CTAs (four per SM; three at 1024,
+// where shared memory holds no more) run the pass 7% faster than 256-thread
+// ones at N = 512 (the same 16 warps per SM), 10% at 256 and 3.5% at 1024;
+// 64-thread CTAs (seven per SM at 512) are 9% slower again.
 template <int N> struct PCfg { static constexpr bool on = false; };
-template <> struct PCfg<32> { static constexpr bool on = true; using P = Plan<8, 8, 2>; };
-template <> struct PCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
-template <> struct PCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 3>; };
-template <> struct PCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
-template <> struct PCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
-template <> struct PCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
-template <> struct PCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
-template <> struct PCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; };
+struct PDef { static constexpr int THREADS = 128, MINB = 4; };
+template <> struct PCfg<32> : PDef { static constexpr bool on = true; using P = Plan<8, 8, 2>; };
+template <> struct PCfg<64> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
+template <> struct PCfg<96> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 3>; };
+template <> struct PCfg<128> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
+template <> struct PCfg<192> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct PCfg<256> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
+template <> struct PCfg<512> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
+template <> struct PCfg<1024> {
+  static constexpr bool on = true;
+  using P = Plan<16, 16, 16, 2>;
+  static constexpr int THREADS = 128, MINB = 3;
+};
 
 template <int N> struct PK {
   using P = typename PCfg<N>::P;
   static constexpr int H = N / 2, E = P::E, G = H / E;
   static_assert(PlanRun<P>::L == H, "line plan length");
   static_assert(E % 2 == 0 && G >= 2 && G <= 32 && 32 % G == 0, "paired line shape");
-  static constexpr int THREADS = 256;
+  static constexpr int THREADS = PCfg<N>::THREADS;
   static constexpr int NG = THREADS / G;                // lines per CTA step
-  static constexpr int MINB = 2;
+  static constexpr int MINB = PCfg<N>::MINB;
+  static_assert(THREADS >= kMaxBatch && THREADS % G == 0, "per-radius sums need a thread per radius");
   static constexpr int gsize = GroupBuf<H, G>::size;
   static constexpr int TW = (PlanRun<P>::TW + 1) & ~1;
   static constexpr int STG = NG * H;                    // one staged step: NG whole lines (float2)
