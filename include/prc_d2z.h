@@ -149,7 +149,7 @@ int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_devic
 
 /* prc_d2z_forward over n boxes of this context's shape, all from host
  * buffers (delta[i] -> zreion[i], argmax[i]; argmax may be null): a stream of
- * realisations, as a driver that loops main_d2z.C:57-71 over input files
+ * realisations, as a program that loops main_d2z.C:57-71 over input files
  * would run it.  Box i+1's input is copied in and box i-1's outputs copied
  * out by the copy engines while box i's kernels run (pinned buffers; pageable
  * ones are correct but serialise).  Results equal n calls of
