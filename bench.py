@@ -344,6 +344,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches,
         "roofline": rl,
         "canonical_3pass_gbs": canon / (ms_step * 1e-3) / 1e9,
+        # compulsory floor: read the spectrum and write the cells once per radius
+        "compulsory_floor_gbs": NR * (8 * Nc + 8 * N ** 3) / (ms_step * 1e-3) / 1e9,
         "clocks": clk.summary(),
     }
     if world == 1 and not args.no_cpu:
