@@ -57,8 +57,9 @@ template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<1
 // exchange buffer, no register prefetch -- 1-2% slower over the whole step.)
 template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
-template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
+template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P, bool TWC_ = false> struct CK {
   using P = P_;
+  static constexpr bool TWC = TWC_;  // computed twiddles (PlanRun TWC)
   static constexpr int H = N / 2, T = T_, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
   static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
@@ -105,18 +106,29 @@ struct CtaSync {
 
 // Window-pass variants (tile width, plan) the autotuner chooses among.
 // Variant 0 is the default (TWIN / PWIN); up to kWinVariants per grid size.
-constexpr int kWinVariants = 3;
-template <int N, int V> struct WinVar { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
+constexpr int kWinVariants = 4;
+template <int N, int V> struct WinVar {
+  static constexpr bool on = false, TWC = false;
+  static constexpr int T = 16;
+  using P = void;
+};
 template <int N> struct WinVar<N, 0> {
-  static constexpr bool on = CCfg<N>::on;
+  static constexpr bool on = CCfg<N>::on, TWC = false;
   static constexpr int T = CCfg<N>::TWIN;
   using P = typename WinPlan<CCfg<N>>::type;
 };
-template <> struct WinVar<128, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
-template <> struct WinVar<256, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<256, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<512, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
-template <> struct WinVar<512, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+struct WV { static constexpr bool on = true, TWC = false; };
+template <> struct WinVar<128, 1> : WV { static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
+template <> struct WinVar<256, 1> : WV { static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<256, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<512, 1> : WV { static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
+template <> struct WinVar<512, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+// the default 512 pass with computed twiddles (fewer shared-memory loads)
+template <> struct WinVar<512, 3> {
+  static constexpr bool on = true, TWC = true;
+  static constexpr int T = 8;
+  using P = Plan<16, 16, 16, 2>;
+};
 
 // Tile width and plan of a mode: the window pass uses its variant V, and the
 // accumulate mode uses variant 0 of the window pass when the plain plan holds
@@ -127,7 +139,8 @@ template <int N, int MODE> struct ColUsesWin {
 };
 template <int N, int MODE, int V> struct ColK {
   static constexpr int VV = MODE == TM_WIN ? V : 0;
-  using type = typename std::conditional<ColUsesWin<N, MODE>::v, CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P>,
+  using type = typename std::conditional<ColUsesWin<N, MODE>::v,
+                                         CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P, WinVar<N, VV>::TWC>,
                                          CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
 };
 
@@ -285,7 +298,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
             gload(wn.sg.in + wn.off, wn.sg.row_stride, raw);
           }
         }
-        PlanRun<P>::template run<true, KK::PP>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<true, KK::PP, KK::TWC>(v, buf, t, tws, sync);
         gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it

@@ -8,7 +8,9 @@ same argmax for every cell whose top-two margin (best vs runner-up radius, or
 vs the initial zreion = 0) exceeds eps_z; the near-barrier fraction is
 reported (about 1% at 512^3 x 64: adjacent radii of a dense log grid give
 close z) and must stay below 5%; the ionisation history x_i(z) of the GPU
-zreion within 1e-4 of that of the FP64 zreion."""
+zreion within 1e-4 of that of the FP64 zreion.  zreion, argmax and x_i are
+checked for the default and for the autotuned radius batch and window-pass
+variant."""
 import math
 
 import numpy as np
@@ -23,11 +25,16 @@ H_ = 0.68
 
 
 @pytest.mark.parametrize("N,box,nr,zeta", [(512, 600.0, 64, 80.5404), (1024, 1200.0, 96, 73.1587)])
-def test_full_size_against_fp64(N, box, nr, zeta):
+def test_full_size_against_fp64(N, box, nr, zeta, tmp_path):
     import torch
+
+    from prc_d2z import autotune
     free, _ = torch.cuda.mem_get_info()
     if free < (12 if N == 512 else 100) * 2 ** 30:
         pytest.skip("not enough device memory for the FP64 restatement")
+    # the autotuned (radius batch, window variant), which the benchmark runs,
+    # is checked beside the default
+    tuned = autotune.tuned(N, nr, path=str(tmp_path / "tune.json"))
     p = prc_d2z.Parameters(N=N, Nscales=nr, BoxSize=box, Rmin=2.0)
     cl = prc_d2z.CLParameters(Rmax=60.0, zeta=zeta, M_min=1e9 / H_)
     delta = fields.gaussian_field(N, box, seed=1, backend="torch").contiguous()
@@ -54,9 +61,19 @@ def test_full_size_against_fp64(N, box, nr, zeta):
         assert bool((dz[clear] <= eps[clear]).all()), float(dz[clear].max())
         assert bool((am[clear] == amo[clear]).all())
         # ionisation history x_i(z) (GetHistory of each field) within 1e-4
-        _, x_gpu, _ = ctx.history(z)
         _, x_64, _ = ctx.history(zo.float().contiguous())
+        _, x_gpu, _ = ctx.history(z)
         dx = float(np.max(np.abs(x_gpu.astype(np.float64) - x_64.astype(np.float64))))
         assert dx <= 1e-4, dx
         print(f"N={N}: near-barrier fraction {frac_near:.2e}, max |dz| on clear cells {float(dz[clear].max()):.3e}, "
+              f"max |dx_i| {dx:.2e}")
+        ctx.tune(*tuned)
+        z, am, _ = ctx.forward(delta)
+        dz = (z.double() - zo).abs()
+        assert bool((dz[clear] <= eps[clear]).all()), (tuned, float(dz[clear].max()))
+        assert bool((am[clear] == amo[clear]).all()), tuned
+        _, x_gpu, _ = ctx.history(z)
+        dx = float(np.max(np.abs(x_gpu.astype(np.float64) - x_64.astype(np.float64))))
+        assert dx <= 1e-4, (tuned, dx)
+        print(f"N={N}, tuned (B, variant) = {tuned}: max |dz| on clear cells {float(dz[clear].max()):.3e}, "
               f"max |dx_i| {dx:.2e}")
