@@ -41,6 +41,10 @@ namespace prc {
 template <int N> struct CCfg { static constexpr bool on = false; };
 template <class C, class = void> struct WinPlan { using type = typename C::P; };
 template <class C> struct WinPlan<C, decltype(void(sizeof(typename C::PWIN)))> { using type = typename C::PWIN; };
+// TWC: computed twiddles in every column pass of the grid size (measured
+// faster at 512: the y pass 2.6%, the window pass 2%); default off
+template <class C, class = void> struct CfgTwc { static constexpr bool v = false; };
+template <class C> struct CfgTwc<C, decltype(void(C::TWC))> { static constexpr bool v = C::TWC; };
 template <class P> struct FirstRadix;
 template <int E, int R0, int... R> struct FirstRadix<Plan<E, R0, R...>> { static constexpr int v = R0; };
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
@@ -50,7 +54,11 @@ template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12
 template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
-template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
+template <> struct CCfg<512> {
+  static constexpr bool on = true, TWC = true;
+  using P = Plan<16, 16, 16, 2>;
+  static constexpr int T = 16, TWIN = 8;
+};
 // N = 1024: 64 lanes x 8 columns in every pass.  (Measured no faster: plain
 // passes on 32 lanes x 16 columns with 32 elements a lane, and on 64 lanes x 16
 // columns in 1024-thread CTAs of 64 registers -- both 128-byte rows, one
@@ -113,7 +121,7 @@ template <int N, int V> struct WinVar {
   using P = void;
 };
 template <int N> struct WinVar<N, 0> {
-  static constexpr bool on = CCfg<N>::on, TWC = false;
+  static constexpr bool on = CCfg<N>::on, TWC = CfgTwc<CCfg<N>>::v;
   static constexpr int T = CCfg<N>::TWIN;
   using P = typename WinPlan<CCfg<N>>::type;
 };
@@ -123,9 +131,9 @@ template <> struct WinVar<256, 1> : WV { static constexpr int T = 16; using P = 
 template <> struct WinVar<256, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
 template <> struct WinVar<512, 1> : WV { static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
 template <> struct WinVar<512, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
-// the default 512 pass with computed twiddles (fewer shared-memory loads)
+// the default 512 pass with the twiddles read from the tables
 template <> struct WinVar<512, 3> {
-  static constexpr bool on = true, TWC = true;
+  static constexpr bool on = true, TWC = false;
   static constexpr int T = 8;
   using P = Plan<16, 16, 16, 2>;
 };
@@ -141,7 +149,7 @@ template <int N, int MODE, int V> struct ColK {
   static constexpr int VV = MODE == TM_WIN ? V : 0;
   using type = typename std::conditional<ColUsesWin<N, MODE>::v,
                                          CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P, WinVar<N, VV>::TWC>,
-                                         CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
+                                         CK<N, CCfg<N>::T, typename CCfg<N>::P, CfgTwc<CCfg<N>>::v>>::type;
 };
 
 template <int N, int MODE, int V = 0>
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         const Where wn = where(tn);
         gload(wn.sg.in + wn.off + yoff, wn.sg.row_stride, nx);
       }
-      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
+      PlanRun<P>::template run<INV, KK::PP, KK::TWC>(v, buf, t, tws, sync);
       gstore(w, w.sg.out + yoff, v);
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = nx[m];
@@ -270,7 +278,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       const Where w = where(ti);
       float2 v[E];
       gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
-      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
+      PlanRun<P>::template run<INV, KK::PP, KK::TWC>(v, buf, t, tws, sync);
       gstore(w, w.sg.out + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
@@ -316,7 +324,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       for (int b = 0; b < a.nb; ++b) {
         float2 v[E];
         gload(w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride, v);
-        PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<false, KK::PP, KK::TWC>(v, buf, t, tws, sync);
         float wv[E];
         wvals(kq, s_kr[b], wv);
 #pragma unroll

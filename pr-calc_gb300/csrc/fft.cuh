@@ -241,10 +241,11 @@ template <int L, int TWS, int Ns, int OFF, int R, int... Rest> struct TwFill<L, 
 // writes the other buffer, which every thread finished reading before the
 // barrier it has just passed).
 // TWC (computed twiddles): a stage with one butterfly a lane (Ns <= G) loads
-// only w^k and forms w^{rk} by repeated multiplication (R - 2 products, two
-// live values); a radix-2 stage with Ns >= G*Q and Ns*R = 16 G loads only w^t
-// and multiplies it by the constants e^{+-2 pi i q/16} (k = t + G q).  Fewer
-// shared-memory loads for more FMAs.
+// only w^k and w^{(R/2)k} and forms the other w^{rk} by repeated
+// multiplication (R - 3 products, two live values; within 3e-7 of exact for
+// R = 16, the table's within 6e-8); a radix-2 stage with Ns >= G*Q and
+// Ns*R = 16 G loads only w^t and multiplies it by the constants
+// e^{+-2 pi i q/16} (k = t + G q).  Fewer shared-memory loads for more FMAs.
 
 template <int L, int E, bool INV, bool SPLIT, bool PP, bool TWC, int Ns, int OFF, int... Rs> struct Stages;
 
@@ -281,12 +282,15 @@ struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF, R, Rest...> {
 #pragma unroll
       for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
       if constexpr (TW_POW) {
+        // anchors w^k and w^{(R/2)k} from the table, the powers between them
+        // by repeated multiplication (at most R/2 - 1 products deep)
         const float2 w1 = twid<INV>(tws[OFF + k]);
         float2 p = w1;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
+          if (r == R / 2 && R > 2) p = twid<INV>(tws[OFF + (R / 2 - 1) * Ns + k]);
           a[r] = cmul(a[r], p);
-          if (r + 1 < R) p = cmul(p, w1);
+          if (r + 1 < R && r + 1 != R / 2) p = cmul(p, w1);
         }
       } else if constexpr (TW_ROT) {
         const float2 c = make_float2(root16_re(q & 15), INV ? root16_im(q & 15) : -root16_im(q & 15));
