@@ -41,10 +41,13 @@ namespace prc {
 template <int N> struct CCfg { static constexpr bool on = false; };
 template <class C, class = void> struct WinPlan { using type = typename C::P; };
 template <class C> struct WinPlan<C, decltype(void(sizeof(typename C::PWIN)))> { using type = typename C::PWIN; };
-// TWC: computed twiddles in every column pass of the grid size (measured
-// faster at 512: the y pass 2.6%, the window pass 2%); default off
+// TWC: computed twiddles in the column passes of the grid size (measured
+// faster at 512: the y pass 2.6%, the window pass 2%; slower at 256); default off
 template <class C, class = void> struct CfgTwc { static constexpr bool v = false; };
 template <class C> struct CfgTwc<C, decltype(void(C::TWC))> { static constexpr bool v = C::TWC; };
+// TWC_WIN: the window pass's own choice where it differs (default: TWC)
+template <class C, class = void> struct CfgTwcWin { static constexpr bool v = CfgTwc<C>::v; };
+template <class C> struct CfgTwcWin<C, decltype(void(C::TWC_WIN))> { static constexpr bool v = C::TWC_WIN; };
 template <class P> struct FirstRadix;
 template <int E, int R0, int... R> struct FirstRadix<Plan<E, R0, R...>> { static constexpr int v = R0; };
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
@@ -63,7 +66,13 @@ template <> struct CCfg<512> {
 // passes on 32 lanes x 16 columns with 32 elements a lane, and on 64 lanes x 16
 // columns in 1024-thread CTAs of 64 registers -- both 128-byte rows, one
 // exchange buffer, no register prefetch -- 1-2% slower over the whole step.)
-template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
+template <> struct CCfg<1024> {
+  // computed twiddles in the plain passes (the y pass 4.5% faster), not in the
+  // window pass (3.6% slower there)
+  static constexpr bool on = true, TWC = true, TWC_WIN = false;
+  using P = Plan<16, 16, 16, 4>;
+  static constexpr int T = 8, TWIN = 8;
+};
 
 template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P, bool TWC_ = false> struct CK {
   using P = P_;
@@ -121,7 +130,7 @@ template <int N, int V> struct WinVar {
   using P = void;
 };
 template <int N> struct WinVar<N, 0> {
-  static constexpr bool on = CCfg<N>::on, TWC = CfgTwc<CCfg<N>>::v;
+  static constexpr bool on = CCfg<N>::on, TWC = CfgTwcWin<CCfg<N>>::v;
   static constexpr int T = CCfg<N>::TWIN;
   using P = typename WinPlan<CCfg<N>>::type;
 };

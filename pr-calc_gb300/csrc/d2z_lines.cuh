@@ -48,7 +48,7 @@ template <> struct PCfg<512> : PDef {
   using P = Plan<16, 16, 16>;
 };
 template <> struct PCfg<1024> {
-  static constexpr bool on = true, TWC = false;
+  static constexpr bool on = true, TWC = true;  // computed twiddles: 1.8% faster here
   using P = Plan<16, 16, 16, 2>;
   static constexpr int THREADS = 128, MINB = 3;
 };
