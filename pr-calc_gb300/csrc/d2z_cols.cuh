@@ -41,13 +41,6 @@ namespace prc {
 template <int N> struct CCfg { static constexpr bool on = false; };
 template <class C, class = void> struct WinPlan { using type = typename C::P; };
 template <class C> struct WinPlan<C, decltype(void(sizeof(typename C::PWIN)))> { using type = typename C::PWIN; };
-// TWC: computed twiddles in the column passes of the grid size (measured
-// faster at 512: the y pass 2.6%, the window pass 2%; slower at 256); default off
-template <class C, class = void> struct CfgTwc { static constexpr bool v = false; };
-template <class C> struct CfgTwc<C, decltype(void(C::TWC))> { static constexpr bool v = C::TWC; };
-// TWC_WIN: the window pass's own choice where it differs (default: TWC)
-template <class C, class = void> struct CfgTwcWin { static constexpr bool v = CfgTwc<C>::v; };
-template <class C> struct CfgTwcWin<C, decltype(void(C::TWC_WIN))> { static constexpr bool v = C::TWC_WIN; };
 template <class P> struct FirstRadix;
 template <int E, int R0, int... R> struct FirstRadix<Plan<E, R0, R...>> { static constexpr int v = R0; };
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
@@ -57,26 +50,15 @@ template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12
 template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
-template <> struct CCfg<512> {
-  static constexpr bool on = true, TWC = true;
-  using P = Plan<16, 16, 16, 2>;
-  static constexpr int T = 16, TWIN = 8;
-};
+template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
 // N = 1024: 64 lanes x 8 columns in every pass.  (Measured no faster: plain
 // passes on 32 lanes x 16 columns with 32 elements a lane, and on 64 lanes x 16
 // columns in 1024-thread CTAs of 64 registers -- both 128-byte rows, one
 // exchange buffer, no register prefetch -- 1-2% slower over the whole step.)
-template <> struct CCfg<1024> {
-  // computed twiddles in the plain passes (the y pass 4.5% faster), not in the
-  // window pass (3.6% slower there)
-  static constexpr bool on = true, TWC = true, TWC_WIN = false;
-  using P = Plan<16, 16, 16, 4>;
-  static constexpr int T = 8, TWIN = 8;
-};
+template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
-template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P, bool TWC_ = false> struct CK {
+template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
   using P = P_;
-  static constexpr bool TWC = TWC_;  // computed twiddles (PlanRun TWC)
   static constexpr int H = N / 2, T = T_, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
   static_assert(G % 2 == 0 && H % T == 0, "column tile shape");
@@ -123,29 +105,18 @@ struct CtaSync {
 
 // Window-pass variants (tile width, plan) the autotuner chooses among.
 // Variant 0 is the default (TWIN / PWIN); up to kWinVariants per grid size.
-constexpr int kWinVariants = 4;
-template <int N, int V> struct WinVar {
-  static constexpr bool on = false, TWC = false;
-  static constexpr int T = 16;
-  using P = void;
-};
+constexpr int kWinVariants = 3;
+template <int N, int V> struct WinVar { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
 template <int N> struct WinVar<N, 0> {
-  static constexpr bool on = CCfg<N>::on, TWC = CfgTwcWin<CCfg<N>>::v;
+  static constexpr bool on = CCfg<N>::on;
   static constexpr int T = CCfg<N>::TWIN;
   using P = typename WinPlan<CCfg<N>>::type;
 };
-struct WV { static constexpr bool on = true, TWC = false; };
-template <> struct WinVar<128, 1> : WV { static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
-template <> struct WinVar<256, 1> : WV { static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<256, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<512, 1> : WV { static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
-template <> struct WinVar<512, 2> : WV { static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
-// the default 512 pass with the twiddles read from the tables
-template <> struct WinVar<512, 3> {
-  static constexpr bool on = true, TWC = false;
-  static constexpr int T = 8;
-  using P = Plan<16, 16, 16, 2>;
-};
+template <> struct WinVar<128, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
+template <> struct WinVar<256, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<256, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<512, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
+template <> struct WinVar<512, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
 
 // Tile width and plan of a mode: the window pass uses its variant V, and the
 // accumulate mode uses variant 0 of the window pass when the plain plan holds
@@ -156,9 +127,8 @@ template <int N, int MODE> struct ColUsesWin {
 };
 template <int N, int MODE, int V> struct ColK {
   static constexpr int VV = MODE == TM_WIN ? V : 0;
-  using type = typename std::conditional<ColUsesWin<N, MODE>::v,
-                                         CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P, WinVar<N, VV>::TWC>,
-                                         CK<N, CCfg<N>::T, typename CCfg<N>::P, CfgTwc<CCfg<N>>::v>>::type;
+  using type = typename std::conditional<ColUsesWin<N, MODE>::v, CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P>,
+                                         CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
 };
 
 template <int N, int MODE, int V = 0>
@@ -275,7 +245,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         const Where wn = where(tn);
         gload(wn.sg.in + wn.off + yoff, wn.sg.row_stride, nx);
       }
-      PlanRun<P>::template run<INV, KK::PP, KK::TWC>(v, buf, t, tws, sync);
+      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
       gstore(w, w.sg.out + yoff, v);
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = nx[m];
@@ -287,7 +257,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       const Where w = where(ti);
       float2 v[E];
       gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
-      PlanRun<P>::template run<INV, KK::PP, KK::TWC>(v, buf, t, tws, sync);
+      PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
       gstore(w, w.sg.out + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
@@ -315,7 +285,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
             gload(wn.sg.in + wn.off, wn.sg.row_stride, raw);
           }
         }
-        PlanRun<P>::template run<true, KK::PP, KK::TWC>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<true, KK::PP>(v, buf, t, tws, sync);
         gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
@@ -333,7 +303,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       for (int b = 0; b < a.nb; ++b) {
         float2 v[E];
         gload(w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride, v);
-        PlanRun<P>::template run<false, KK::PP, KK::TWC>(v, buf, t, tws, sync);
+        PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
         float wv[E];
         wvals(kq, s_kr[b], wv);
 #pragma unroll

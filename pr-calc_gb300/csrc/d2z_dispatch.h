@@ -6,7 +6,7 @@
 
 namespace prc {
 
-constexpr int kMaxWinVariants = 4;  // window-pass variants per grid size (autotuned)
+constexpr int kMaxWinVariants = 3;  // window-pass variants per grid size (autotuned)
 
 struct TileArgs;
 struct SweepArgs;

@@ -33,22 +33,16 @@ namespace prc {
 // ones at N = 512 (the same 16 warps per SM), 10% at 256 and 3.5% at 1024;
 // 64-thread CTAs (seven per SM at 512) are 9% slower again.
 template <int N> struct PCfg { static constexpr bool on = false; };
-struct PDef {
-  static constexpr int THREADS = 128, MINB = 4;
-  static constexpr bool TWC = false;  // computed twiddles (PlanRun TWC)
-};
+struct PDef { static constexpr int THREADS = 128, MINB = 4; };
 template <> struct PCfg<32> : PDef { static constexpr bool on = true; using P = Plan<8, 8, 2>; };
 template <> struct PCfg<64> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
 template <> struct PCfg<96> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 3>; };
 template <> struct PCfg<128> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
 template <> struct PCfg<192> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
 template <> struct PCfg<256> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
-template <> struct PCfg<512> : PDef {
-  static constexpr bool on = true, TWC = true;  // computed twiddles: 1.2% faster here
-  using P = Plan<16, 16, 16>;
-};
+template <> struct PCfg<512> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
 template <> struct PCfg<1024> {
-  static constexpr bool on = true, TWC = true;  // computed twiddles: 1.8% faster here
+  static constexpr bool on = true;
   using P = Plan<16, 16, 16, 2>;
   static constexpr int THREADS = 128, MINB = 3;
 };
@@ -235,7 +229,7 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
       const float2 xo = cmul(csub(xm, xc), tw[H / 2]);
       v[EH] = make_float2(xe.x - xo.y, xe.y + xo.x);
     }
-    PlanRun<P>::template run<true, false, PCfg<N>::TWC>(v, buf, t, tws, sync);
+    PlanRun<P>::template run<true>(v, buf, t, tws, sync);
     const float cb = s_cb[b];
     const uint32_t rid = (uint32_t)(a.r0 + b);
     float ss = 0.f;

@@ -43,15 +43,6 @@ template <bool INV> __device__ __forceinline__ float2 twid(float2 w) {
 #define PRC_COS_PI8 0.92387953251128675613f
 #define PRC_SIN_PI8 0.38268343236508977173f
 
-// e^{+2 pi i m/16}, m = 0..15, from the closed forms above
-__device__ __forceinline__ constexpr float root16_re(int m) {
-  constexpr float c[4] = {1.0f, PRC_COS_PI8, PRC_SQRT1_2, PRC_SIN_PI8};  // cos(2 pi m/16), m = 0..3
-  const int q = m & 3, h = (m >> 2) & 3;  // m = 4h + q
-  // cos(2 pi (4h + q)/16) = cos(pi h/2 + 2 pi q/16)
-  return h == 0 ? c[q] : h == 1 ? (q == 0 ? 0.0f : -c[4 - q]) : h == 2 ? -c[q] : (q == 0 ? 0.0f : c[4 - q]);
-}
-__device__ __forceinline__ constexpr float root16_im(int m) { return root16_re((m + 12) & 15); }  // sin x = cos(x - pi/2)
-
 // ---------------------------------------------------------------- small DFTs
 template <int R, bool INV> struct Dft;
 
@@ -240,23 +231,15 @@ template <int L, int TWS, int Ns, int OFF, int R, int... Rest> struct TwFill<L, 
 // each exchange, so one barrier per exchange suffices (the next exchange
 // writes the other buffer, which every thread finished reading before the
 // barrier it has just passed).
-// TWC (computed twiddles): a stage with one butterfly a lane (Ns <= G) loads
-// only w^k and w^{(R/2)k} and forms the other w^{rk} by repeated
-// multiplication (R - 3 products, two live values; within 3e-7 of exact for
-// R = 16, the table's within 6e-8); a radix-2 stage with Ns >= G*Q and
-// Ns*R = 16 G loads only w^t and multiplies it by the constants
-// e^{+-2 pi i q/16} (k = t + G q).  Fewer shared-memory loads for more FMAs.
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF, int... Rs> struct Stages;
 
-template <int L, int E, bool INV, bool SPLIT, bool PP, bool TWC, int Ns, int OFF, int... Rs> struct Stages;
-
-template <int L, int E, bool INV, bool SPLIT, bool PP, bool TWC, int Ns, int OFF>
-struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF> {
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF> struct Stages<L, E, INV, SPLIT, PP, Ns, OFF> {
   template <class Buf, class Sync>
   static __device__ __forceinline__ void run(float2 (&)[E], Buf&, int, const float2*, const Sync&) {}
 };
 
-template <int L, int E, bool INV, bool SPLIT, bool PP, bool TWC, int Ns, int OFF, int R, int... Rest>
-struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF, R, Rest...> {
+template <int L, int E, bool INV, bool SPLIT, bool PP, int Ns, int OFF, int R, int... Rest>
+struct Stages<L, E, INV, SPLIT, PP, Ns, OFF, R, Rest...> {
   template <class Buf, class Sync>
   static __device__ __forceinline__ void run(float2 (&v)[E], Buf& buf, int t, const float2* tws,
                                              const Sync& sync) {
@@ -270,10 +253,6 @@ struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF, R, Rest...> {
     // G*(q%NG) + r*Ns.
     int hw = 0;
     if constexpr (SPLIT && !last) hw = buf.thread(Ns <= G ? (t / Ns) * Ns * R + (t % Ns) : t);
-    constexpr bool TW_POW = TWC && Ns > 1 && Ns <= G && Q == 1;
-    constexpr bool TW_ROT = TWC && R == 2 && Ns > G && Ns >= G * Q && Ns * R == 16 * G;
-    float2 wt = make_float2(1.f, 0.f);
-    if constexpr (TW_ROT) wt = twid<INV>(tws[OFF + t]);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int j = t + G * q;
@@ -281,21 +260,7 @@ struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF, R, Rest...> {
       float2 a[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
-      if constexpr (TW_POW) {
-        // anchors w^k and w^{(R/2)k} from the table, the powers between them
-        // by repeated multiplication (at most R/2 - 1 products deep)
-        const float2 w1 = twid<INV>(tws[OFF + k]);
-        float2 p = w1;
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          if (r == R / 2 && R > 2) p = twid<INV>(tws[OFF + (R / 2 - 1) * Ns + k]);
-          a[r] = cmul(a[r], p);
-          if (r + 1 < R && r + 1 != R / 2) p = cmul(p, w1);
-        }
-      } else if constexpr (TW_ROT) {
-        const float2 c = make_float2(root16_re(q & 15), INV ? root16_im(q & 15) : -root16_im(q & 15));
-        a[1] = cmul(a[1], q == 0 ? wt : cmul(wt, c));
-      } else if constexpr (Ns > 1) {
+      if constexpr (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) a[r] = cmul(a[r], twid<INV>(tws[OFF + (r - 1) * Ns + k]));
       }
@@ -325,7 +290,7 @@ struct Stages<L, E, INV, SPLIT, PP, TWC, Ns, OFF, R, Rest...> {
       }
       if constexpr (PP) buf.flip();
       else sync();
-      Stages<L, E, INV, SPLIT, PP, TWC, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(v, buf, t, tws, sync);
+      Stages<L, E, INV, SPLIT, PP, Ns * R, OFF + (Ns > 1 ? (R - 1) * Ns : 0), Rest...>::run(v, buf, t, tws, sync);
     }
   }
 };
@@ -341,10 +306,10 @@ template <int E, int... R> struct PlanRun<Plan<E, R...>> {
   static __device__ __forceinline__ void fill(float2* tws, const float2* tabN) {
     TwFill<L, TWS, 1, 0, R...>::run(tws, tabN);
   }
-  template <bool INV, bool PP = false, bool TWC = false, class Buf, class Sync>
+  template <bool INV, bool PP = false, class Buf, class Sync>
   static __device__ __forceinline__ void run(float2 (&v)[E], Buf& buf, int t, const float2* tws,
                                              const Sync& sync) {
-    Stages<L, E, INV, SPLIT, PP, TWC, 1, 0, R...>::run(v, buf, t, tws, sync);
+    Stages<L, E, INV, SPLIT, PP, 1, 0, R...>::run(v, buf, t, tws, sync);
   }
 };
 
