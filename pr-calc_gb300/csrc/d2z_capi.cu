@@ -742,52 +742,61 @@ int prc_d2z_forward_many(prc_d2z_ctx* c, int n, const float* const* delta, float
   cudaStream_t cin = c->m_copy[0], cout = c->m_copy[1];
   c->launches = 0;
   c->have_timing = 0;
-  // the first input copies may not overtake work already queued on the stream
-  PRC_CU(cudaEventRecord(c->m_read[0], c->st), "event");
-  PRC_CU(cudaEventRecord(c->m_read[1], c->st), "event");
-  PRC_CU(cudaEventRecord(c->m_out[0], c->st), "event");
-  PRC_CU(cudaEventRecord(c->m_out[1], c->st), "event");
-  for (int i = 0; i < n; ++i) {
-    const int k = i & 1;
-    // the first box has nothing to overlap its input copy with: a mapped
-    // input is read in place by its R2C instead; likewise the last box's
-    // final sweep writes mapped outputs in place
-    const float* d_in = (i == 0) ? static_cast<const float*>(mapped_view(delta[0])) : nullptr;
-    float* z_fin = nullptr;
-    uint8_t* am_fin = nullptr;
-    // (not when the previous box copies into the same buffer: that copy is
-    // ordered on the output stream only)
-    const bool reused = i > 0 && (zreion[i] == zreion[i - 1] || (want_am && argmax[i] == argmax[i - 1]));
-    if (i == n - 1 && !reused) {
-      z_fin = static_cast<float*>(mapped_view(zreion[i]));
-      am_fin = want_am ? static_cast<uint8_t*>(mapped_view(argmax[i])) : nullptr;
-      if (want_am && !am_fin) z_fin = nullptr;
+  // everything is queued by enqueue(); whatever it returns, the three streams
+  // are drained before the call returns, so no copy touches a caller's buffer
+  // afterwards
+  auto enqueue = [&]() -> int {
+    // the first input copies may not overtake work already queued on the stream
+    PRC_CU(cudaEventRecord(c->m_read[0], c->st), "event");
+    PRC_CU(cudaEventRecord(c->m_read[1], c->st), "event");
+    PRC_CU(cudaEventRecord(c->m_out[0], c->st), "event");
+    PRC_CU(cudaEventRecord(c->m_out[1], c->st), "event");
+    for (int i = 0; i < n; ++i) {
+      const int k = i & 1;
+      // the first box has nothing to overlap its input copy with: a mapped
+      // input is read in place by its R2C instead; likewise the last box's
+      // final sweep writes mapped outputs in place
+      const float* d_in = (i == 0) ? static_cast<const float*>(mapped_view(delta[0])) : nullptr;
+      float* z_fin = nullptr;
+      uint8_t* am_fin = nullptr;
+      // (not when the previous box copies into the same buffer: that copy is
+      // ordered on the output stream only)
+      const bool reused = i > 0 && (zreion[i] == zreion[i - 1] || (want_am && argmax[i] == argmax[i - 1]));
+      if (i == n - 1 && !reused) {
+        z_fin = static_cast<float*>(mapped_view(zreion[i]));
+        am_fin = want_am ? static_cast<uint8_t*>(mapped_view(argmax[i])) : nullptr;
+        if (want_am && !am_fin) z_fin = nullptr;
+      }
+      if (!d_in) {
+        // after the previous box's R2C: it may be reading its input over the
+        // host link, and the box before it (same buffer) is past its R2C too
+        PRC_CU(cudaStreamWaitEvent(cin, c->m_read[i == 0 ? k : (i - 1) & 1], 0), "wait");
+        PRC_CU(copy_chunked(c->m_delta[k], delta[i], sizeof(float) * n3, cudaMemcpyHostToDevice, cin), "H2D delta");
+        PRC_CU(cudaEventRecord(c->m_in[k], cin), "event");
+        PRC_CU(cudaStreamWaitEvent(c->st, c->m_in[k], 0), "wait");
+        d_in = c->m_delta[k];
+      }
+      PRC_CU(cudaStreamWaitEvent(c->st, c->m_out[k], 0), "wait");
+      forward_r2c(c, d_in, c->dinit);
+      PRC_CU(cudaEventRecord(c->m_read[k], c->st), "event");
+      enqueue_sweeps(c, c->m_z[k], want_am ? c->m_am[k] : nullptr, nullptr, z_fin, am_fin);
+      PRC_CU(cudaGetLastError(), "kernel launch");
+      PRC_CU(cudaEventRecord(c->m_done[k], c->st), "event");
+      if (!z_fin) {
+        PRC_CU(cudaStreamWaitEvent(cout, c->m_done[k], 0), "wait");
+        PRC_CU(copy_chunked(zreion[i], c->m_z[k], sizeof(float) * n3, cudaMemcpyDeviceToHost, cout), "D2H zreion");
+        if (want_am)
+          PRC_CU(copy_chunked(argmax[i], c->m_am[k], (size_t)n3, cudaMemcpyDeviceToHost, cout), "D2H argmax");
+        PRC_CU(cudaEventRecord(c->m_out[k], cout), "event");
+      }
     }
-    if (!d_in) {
-      // after the previous box's R2C: it may be reading its input over the
-      // host link, and the box before it (same buffer) is past its R2C too
-      PRC_CU(cudaStreamWaitEvent(cin, c->m_read[i == 0 ? k : (i - 1) & 1], 0), "wait");
-      PRC_CU(copy_chunked(c->m_delta[k], delta[i], sizeof(float) * n3, cudaMemcpyHostToDevice, cin), "H2D delta");
-      PRC_CU(cudaEventRecord(c->m_in[k], cin), "event");
-      PRC_CU(cudaStreamWaitEvent(c->st, c->m_in[k], 0), "wait");
-      d_in = c->m_delta[k];
-    }
-    PRC_CU(cudaStreamWaitEvent(c->st, c->m_out[k], 0), "wait");
-    forward_r2c(c, d_in, c->dinit);
-    PRC_CU(cudaEventRecord(c->m_read[k], c->st), "event");
-    enqueue_sweeps(c, c->m_z[k], want_am ? c->m_am[k] : nullptr, nullptr, z_fin, am_fin);
-    PRC_CU(cudaGetLastError(), "kernel launch");
-    PRC_CU(cudaEventRecord(c->m_done[k], c->st), "event");
-    if (!z_fin) {
-      PRC_CU(cudaStreamWaitEvent(cout, c->m_done[k], 0), "wait");
-      PRC_CU(copy_chunked(zreion[i], c->m_z[k], sizeof(float) * n3, cudaMemcpyDeviceToHost, cout), "D2H zreion");
-      if (want_am)
-        PRC_CU(copy_chunked(argmax[i], c->m_am[k], (size_t)n3, cudaMemcpyDeviceToHost, cout), "D2H argmax");
-      PRC_CU(cudaEventRecord(c->m_out[k], cout), "event");
-    }
-  }
-  PRC_CU(cudaStreamSynchronize(cout), "prc_d2z_forward_many");
-  PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_forward_many");
+    return PRC_OK;
+  };
+  st = enqueue();
+  const cudaError_t e0 = cudaStreamSynchronize(cin), e1 = cudaStreamSynchronize(cout),
+                    e2 = cudaStreamSynchronize(c->st);
+  if (st != PRC_OK) return st;
+  PRC_CU(e0 != cudaSuccess ? e0 : (e1 != cudaSuccess ? e1 : e2), "prc_d2z_forward_many");
   if ((st = check_kernel_flag(c, "prc_d2z_forward_many")) != PRC_OK) return st;
   prof_collect(c);
   return PRC_OK;
