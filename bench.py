@@ -17,9 +17,17 @@ radii (window, C2R, barrier, running max) into zreion.
 Multi-GPU (torchrun): replicas, one box per rank, no collective on the data
 path; value = all ranks' cell*radii / max-over-ranks time.
 
+The default line also carries the rest of the headline metric, each timed
+with CUDA events under its own clock record: "adjoint" (backward / forward
+time at 256^3 x 64, loss mean((z - z_t)^2)), "batched" (96 boxes of
+64..256^3 in one captured launch against a per-box loop of the plain path,
+bit-identity checked) and "step_frac" (the whole step's rate on the kernels'
+own algorithmic bytes, on the compulsory floor and on the canonical 3-pass
+model, each against the measured HBM copy rate).
+
 --impl reference times the CPU implementation of the same step (the oracle's
 faithful-fp32 restatement: scipy.fft with all host threads plus the OpenMP
-C loops of oracle/d2z_cells.c) on a bounded sample per step.
+C loops of oracle/d2z_cells.c): every step is a whole step, all radii.
 """
 from __future__ import annotations
 
@@ -46,7 +54,6 @@ MMIN_MSUN = 1e9 / H_
 # zeta from prc_d2z.calibrate: raw zreion with x_i(z=8) = 0.5 at seed 1
 ZETA = 80.5404       # 512^3, 600 Mpc/h, 64 radii to 60 Mpc/h
 ZETA_BATCH = 81.6855 # 256^3, 384 Mpc/h (1.5 Mpc/h cells), 48 radii to 60 Mpc/h
-CPU_SAMPLE_RADII = 4
 # plain configurations: N, box [Mpc/h], radii, calibrated zeta (x_i(z=8) = 0.5 at seed 1)
 CONFIGS = {"C1": (128, 200.0, 32, 82.4429), "C2": (512, 600.0, 64, 80.5404), "C3": (1024, 1200.0, 96, 73.1587)}
 
@@ -124,6 +131,12 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _config(N, box):
+    """The workload keys, identical in both arms' lines."""
+    return {"workload": f"plain delta2zreion {N}^3, {box:g} Mpc/h, {NR} radii", "N": N, "radii": NR,
+            "box_mpc_h": box, "zeta": ZETA, "l2": "inputs larger than L2 (no flush)"}
+
+
 def _algo_bytes(kind, N, nb, first):
     """Algorithmic DRAM bytes of one launch (what the kernel must read + write)."""
     Nc = N * N * (N // 2 + 1)
@@ -153,9 +166,21 @@ def _traffic(kind, N):
     return None
 
 
+def _step_bytes(N, B):
+    """Algorithmic bytes of one whole step as these kernels move them: the
+    forward R2C (z pass, two column passes), then per sweep of up to B radii
+    the window + x pass, the y pass and the z pass with the running max."""
+    Nc = N * N * (N // 2 + 1)
+    tot = _algo_bytes("r2c_z", N, 1, True) + 2 * _algo_bytes("col_fwd", N, 1, True)
+    for s, r0 in enumerate(range(0, NR, B)):
+        nb = min(B, NR - r0)
+        tot += sum(_algo_bytes(k, N, nb, s == 0) for k in ("win_x", "col_inv", "c2r_z"))
+    return tot, NR * (8 * Nc + 8 * N ** 3), NR * (40 * Nc + 8 * N ** 3) + 4 * N ** 3 + 40 * Nc
+
+
 def cpu_sample(delta_np, tables, box_mpc, n_radii_sample, threads):
-    """Oracle (faithful fp32) on a bounded sample: forward + n radii; returns
-    the extrapolated full-workload cell*radii/s and the timings."""
+    """Oracle (faithful fp32): forward + n radii (all NR: one whole step);
+    returns the full-workload cell*radii/s and the timings."""
     from oracle import d2z_ref as orc
     orc.lib().orc_set_threads(threads)
     N = delta_np.shape[0]
@@ -193,20 +218,26 @@ def run_reference(args, rank):
     delta = fields.gaussian_field(N, p.BoxSize, seed=1)
     box_mpc = float(np.float32(p.BoxSize) / np.float32(H_))
     vals = []
-    for s in range(args.warmup + args.steps):
-        v, tf, tr = cpu_sample(delta, T, box_mpc, args.ref_radii, threads)
-        if s >= args.warmup:
-            vals.append((v, tf, tr))
+    for s in range(args.warmup):  # warm-up: the FFT plans, thread pools and caches (not timed)
+        cpu_sample(delta, T, box_mpc, 2, threads)
+    for s in range(args.steps):
+        vals.append(cpu_sample(delta, T, box_mpc, args.ref_radii or NR, threads))
     v = statistics.median(x[0] for x in vals)
     ms = N ** 3 * NR / v * 1e3
-    sample = (f"forward R2C + {args.ref_radii} of {NR} radii per step at {N}^3, extrapolated to all {NR} radii "
-              f"(t_fwd {statistics.median(x[1] for x in vals):.2f} s, t_radius {statistics.median(x[2] for x in vals):.2f} s)")
+    nr_s = args.ref_radii or NR
+    if nr_s >= NR:
+        sample = (f"whole steps: forward R2C + all {NR} radii at {N}^3 "
+                  f"(t_fwd {statistics.median(x[1] for x in vals):.2f} s, "
+                  f"t_radius {statistics.median(x[2] for x in vals):.3f} s)")
+    else:
+        sample = (f"forward R2C + {nr_s} of {NR} radii per step at {N}^3, extrapolated to all {NR} radii "
+                  f"(t_fwd {statistics.median(x[1] for x in vals):.2f} s, "
+                  f"t_radius {statistics.median(x[2] for x in vals):.3f} s)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox4x32-10 + BBKS, seed 1)",
-        "config": {"workload": f"plain delta2zreion {N}^3, {p.BoxSize:g} Mpc/h, {NR} radii", "N": N,
-                   "radii": NR, "box_mpc_h": p.BoxSize, "zeta": ZETA, "l2": "inputs larger than L2"},
+        "config": _config(N, p.BoxSize), "parallelism": f"{threads} host threads",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -327,27 +358,37 @@ def run_ours(args, rank, world, local_rank):
           "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
           "bytes_per_launch": bytes_launch, "ms_per_launch": per_launch_ms,
           "kernel_share": {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items() if v[1]}}
-    # canonical 3-pass model bytes (40 Nc + 8 N^3 per radius, 4 N^3 + 40 Nc once)
-    Nc = N * N * (N // 2 + 1)
-    canon = NR * (40 * Nc + 8 * N ** 3) + 4 * N ** 3 + 40 * Nc
+    # the whole step against the measured copy rate, on three byte counts: the
+    # kernels' own algorithmic bytes, the compulsory floor (read the spectrum
+    # and write the cells once per radius) and the canonical 3-pass model
+    # (40 Nc + 8 N^3 per radius, 4 N^3 + 40 Nc once)
+    own, floor, canon = _step_bytes(N, B)
+    step_s = ms_step * 1e-3
+    step_frac = {"own_bytes": own, "own_gbs": own / step_s / 1e9, "own_frac": own / step_s / 1e9 / peak,
+                 "floor_bytes": floor, "floor_gbs": floor / step_s / 1e9, "floor_frac": floor / step_s / 1e9 / peak,
+                 "canonical_bytes": canon, "canonical_gbs": canon / step_s / 1e9,
+                 "canonical_frac": canon / step_s / 1e9 / peak, "peak_gbs": peak, "peak_source": peak_kind}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox4x32-10 + BBKS, seed 1+rank)",
-        "config": {"workload": f"plain delta2zreion {N}^3, {p.BoxSize:g} Mpc/h, {NR} radii", "N": N,
-                   "radii": NR, "box_mpc_h": p.BoxSize, "zeta": ZETA, "radius_batch": B,
-                   "win_variant": tuned[1] if tuned else 0, "autotuned": tuned is not None,
-                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
+        "config": _config(N, p.BoxSize), "parallelism": f"replicas x{world}",
+        "tuning": {"radius_batch": B, "win_variant": tuned[1] if tuned else 0, "autotuned": tuned is not None},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * N ** 3, "d2h_bytes_per_step": 4 * N ** 3,
                 "api": "prc_d2z_forward_many (K boxes, pinned host buffers, copies overlapped)",
                 "single_call_value": e2e_single, "copy_engine_gbs": copy_gbs},
         "gpu_launches": launches,
         "roofline": rl,
-        "canonical_3pass_gbs": canon / (ms_step * 1e-3) / 1e9,
-        # compulsory floor: read the spectrum and write the cells once per radius
-        "compulsory_floor_gbs": NR * (8 * Nc + 8 * N ** 3) / (ms_step * 1e-3) / 1e9,
+        "step_frac": step_frac,
         "clocks": clk.summary(),
     }
+    ctx.close()
+    del zreion, h_delta, h_z, hd, hz
+    torch.cuda.empty_cache()
+    if world == 1 and not args.no_extras:
+        # the metric's other two parts, each under its own clock record
+        out["adjoint"] = adjoint_measure(256, steps=5, warmup=3)
+        out["batched"] = batched_measure(steps=5, warmup=3, streams=0)
     if world == 1 and not args.no_cpu:
         from oracle import d2z_ref as orc  # noqa: F401
         threads = os.cpu_count() or 1
@@ -356,10 +397,10 @@ def run_ours(args, rank, world, local_rank):
         class T:
             DInit, radii_mpc, barrier_a, barrier_b = t.DInit, t.radii_mpc, t.barrier_a, t.barrier_b
 
-        v, tf, tr = cpu_sample(d_np, T, float(np.float32(p.BoxSize) / np.float32(H_)), CPU_SAMPLE_RADII, threads)
+        v, tf, tr = cpu_sample(d_np, T, float(np.float32(p.BoxSize) / np.float32(H_)), NR, threads)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                               "sample": f"oracle fp32: forward R2C ({tf:.2f} s) + {CPU_SAMPLE_RADII} of {NR} radii "
-                                         f"({tr:.2f} s each) at {N}^3, extrapolated to {NR} radii"}
+                               "sample": f"oracle fp32, one whole step: forward R2C ({tf:.2f} s) + all {NR} radii "
+                                         f"({tr:.3f} s each) at {N}^3"}
     print(json.dumps(out), flush=True)
 
 
@@ -373,11 +414,12 @@ def _cfg_box(N, nr, seed, zeta, box=None, rmax=RMAX):
                 barrier_b=t.barrier_b, barrier_a=t.barrier_a, growth_init=t.DInit), box
 
 
-def run_batched(args):
+def batched_measure(steps, warmup, streams):
     """96 realisations, grids 64/96/128/192/256 at 1.5 Mpc/h cells, 24-48 radii
     each: per-box loop of the plain path vs one captured-graph batch launch.
     Both use the autotuned radius batch and window-pass variant of each grid
-    size (prc_d2z.autotune); the batch also picks its stream count by timing."""
+    size (prc_d2z.autotune); the batch also picks its stream count by timing.
+    Returns a dict (times, speed-up, bit-identity, clocks)."""
     import torch
 
     import prc_d2z
@@ -419,7 +461,6 @@ def run_batched(args):
         bt.forward(deltas, outs_batch, use_graph=True)
 
     stream_ms = None
-    streams = args.streams
     if streams <= 0:
         streams, stream_ms = autotune.tune_batch_streams(make_batch, run_batch, streams=(1, 2, 4))
     batch = make_batch(streams)
@@ -429,49 +470,61 @@ def run_batched(args):
 
     res = {}
     for name, fn in (("loop", loop), ("batched", batched)):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with Clocks(0) as clk:
             e0.record()
-            for _ in range(args.steps):
+            for _ in range(steps):
                 fn()
             e1.record()
             torch.cuda.synchronize()
-        res[name] = (e0.elapsed_time(e1) / args.steps, clk.summary())
+        res[name] = (e0.elapsed_time(e1) / steps, clk.summary())
     same = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_batch))
     ms_loop, ms_b = res["loop"][0], res["batched"][0]
-    print(json.dumps({
-        "metric": "batched zreion cell*radii/s (96 boxes, 64-256^3, 24-48 radii)", "value": work / (ms_b * 1e-3),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (Philox4x32-10 + BBKS, seeds 1000..1095)",
-        "config": {"workload": "batched: 96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
-                               "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
-                   "streams": streams, "graph": True,
-                   "autotuned": {str(N): {"radius_batch": B, "win_variant": v} for N, (B, v) in tuning.items()},
-                   "streams_ms": stream_ms},
-        "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3)},
-        "speedup_vs_loop": ms_loop / ms_b, "identical_to_loop": bool(same),
-        "gpu_launches": batch.launches(), "clocks": res["batched"][1]}), flush=True)
+    out = {"workload": "96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
+                       "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
+           "steps": steps, "warmup": warmup, "ms_per_step": ms_b, "value": work / (ms_b * 1e-3), "unit": UNIT,
+           "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3), "clocks": res["loop"][1]},
+           "speedup_vs_loop": ms_loop / ms_b, "identical_to_loop": bool(same),
+           "streams": streams, "graph": True, "streams_ms": stream_ms,
+           "autotuned": {str(N): {"radius_batch": B, "win_variant": v} for N, (B, v) in tuning.items()},
+           "gpu_launches": batch.launches(), "clocks": res["batched"][1]}
     batch.close()
     for c in ctxs:
         c.close()
+    del deltas, outs_loop, outs_batch
+    torch.cuda.empty_cache()
+    return out
 
 
-def run_adjoint(args):
-    """Adjoint at N^3 with 64 radii: loss = mean((z - z_t)^2), z_t from seed 2;
-    forward (with argmax) and backward timed; ratio t_bwd / t_fwd."""
+def run_batched(args):
+    r = batched_measure(args.steps, args.warmup, args.streams)
+    print(json.dumps({
+        "metric": "batched zreion cell*radii/s (96 boxes, 64-256^3, 24-48 radii)", "value": r["value"],
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Philox4x32-10 + BBKS, seeds 1000..1095)",
+        "config": {"workload": "batched: " + r["workload"], "zeta": ZETA_BATCH},
+        "per_box_loop": r["per_box_loop"], "speedup_vs_loop": r["speedup_vs_loop"],
+        "identical_to_loop": r["identical_to_loop"], "streams": r["streams"], "autotuned": r["autotuned"],
+        "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}), flush=True)
+
+
+def adjoint_measure(N, steps, warmup, batch=0):
+    """Adjoint at N^3 with 64 radii and the 512^3 workload's cell size:
+    loss = mean((z - z_t)^2), z_t from seed 2; forward (with argmax) and
+    backward timed with CUDA events; returns a dict with t_bwd / t_fwd."""
     import torch
 
     import prc_d2z
     from prc_d2z import fields
-    N = args.n
-    box = BOX * N / N_DEF
-    p = prc_d2z.Parameters(N=N, Nscales=NR, BoxSize=box, Rmin=RMIN_CELLS)
-    cl = prc_d2z.CLParameters(Rmax=RMAX, zeta=ZETA, M_min=MMIN_MSUN)
-    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=args.batch, argmax=True)
+    box = 600.0 * N / 512
+    nr, zeta = 64, CONFIGS["C2"][3]
+    p = prc_d2z.Parameters(N=N, Nscales=nr, BoxSize=box, Rmin=RMIN_CELLS)
+    cl = prc_d2z.CLParameters(Rmax=RMAX, zeta=zeta, M_min=MMIN_MSUN)
+    ctx = prc_d2z.Delta2Zreion.from_parameters(p, cl, radius_batch=batch, argmax=True)
     delta = fields.gaussian_field(N, box, seed=1, backend="torch").contiguous()
     target = fields.gaussian_field(N, box, seed=2, backend="torch").contiguous()
     zt, _, _ = ctx.forward(target, want_argmax=False)
@@ -480,34 +533,44 @@ def run_adjoint(args):
     am = torch.empty(delta.shape, dtype=torch.uint8, device=delta.device)
     grad = torch.empty_like(delta)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.forward(delta, zreion=z, argmax=am)
         g = (2.0 / N ** 3) * (z - zt)
         ctx.backward(g, am, dL_ddelta=grad)
     torch.cuda.synchronize()
     tf = tb = 0.0
-    for _ in range(args.steps):
-        ev[0].record()
-        ctx.forward(delta, zreion=z, argmax=am)
-        ev[1].record()
-        g = (2.0 / N ** 3) * (z - zt)
-        ev[2].record()
-        ctx.backward(g, am, dL_ddelta=grad)
-        ev[3].record()
-        torch.cuda.synchronize()
-        tf += ev[0].elapsed_time(ev[1])
-        tb += ev[2].elapsed_time(ev[3])
-    tf /= args.steps
-    tb /= args.steps
+    with Clocks(torch.cuda.current_device()) as clk:
+        for _ in range(steps):
+            ev[0].record()
+            ctx.forward(delta, zreion=z, argmax=am)
+            ev[1].record()
+            g = (2.0 / N ** 3) * (z - zt)
+            ev[2].record()
+            ctx.backward(g, am, dL_ddelta=grad)
+            ev[3].record()
+            torch.cuda.synchronize()
+            tf += ev[0].elapsed_time(ev[1])
+            tb += ev[2].elapsed_time(ev[3])
+    tf /= steps
+    tb /= steps
+    ctx.close()
+    del delta, target, zt, z, am, grad
+    torch.cuda.empty_cache()
+    return {"workload": f"adjoint {N}^3, {box:g} Mpc/h, 64 radii, loss mean((z-z_t)^2)", "N": N,
+            "ratio": tb / tf, "forward_ms": tf, "backward_ms": tb, "steps": steps, "warmup": warmup,
+            "backward_cell_radii_per_s": N ** 3 * nr / (tb * 1e-3), "clocks": clk.summary()}
+
+
+def run_adjoint(args):
+    r = adjoint_measure(args.n, args.steps, args.warmup, args.batch)
     print(json.dumps({
-        "metric": f"adjoint/forward time ratio at {N}^3 (64 radii)", "value": tb / tf, "unit": "ratio",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tf + tb,
+        "metric": f"adjoint/forward time ratio at {args.n}^3 (64 radii)", "value": r["ratio"], "unit": "ratio",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["forward_ms"] + r["backward_ms"],
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (Philox4x32-10 + BBKS, field seed 1, target seed 2)",
-        "config": {"workload": f"adjoint {N}^3, {box:g} Mpc/h, 64 radii, loss mean((z-z_t)^2)", "zeta": ZETA},
-        "forward_ms": tf, "backward_ms": tb,
-        "backward_cell_radii_per_s": N ** 3 * NR / (tb * 1e-3)}), flush=True)
-    ctx.close()
+        "config": {"workload": r["workload"], "zeta": CONFIGS["C2"][3]},
+        "forward_ms": r["forward_ms"], "backward_ms": r["backward_ms"],
+        "backward_cell_radii_per_s": r["backward_cell_radii_per_s"], "clocks": r["clocks"]}), flush=True)
 
 
 def main():
@@ -519,8 +582,9 @@ def main():
     ap.add_argument("--config", default="C2", choices=sorted(CONFIGS))
     ap.add_argument("--n", type=int, default=0, help="grid side (default: the config's; keeps its cell size)")
     ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--ref-radii", type=int, default=2)
+    ap.add_argument("--ref-radii", type=int, default=0, help="reference arm: radii per step (0: all, a whole step)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="default line without the adjoint and batched parts")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
     ap.add_argument("--streams", type=int, default=0, help="batched: streams (0: autotuned)")
     args = ap.parse_args()

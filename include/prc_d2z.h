@@ -43,6 +43,14 @@ extern "C" {
 /* ---- flags for prc_d2z_desc.flags --------------------------------------- */
 #define PRC_FLAG_ARGMAX      1   /* keep the per-cell winning radius index    */
 #define PRC_FLAG_SIGMA_GRID  2   /* per-radius sqrt(<delta_R^2>) diagnostic   */
+/* The window in the reference's own float arithmetic, operation by operation
+ * (delta2zreion_d2z.C:41-43,59-82: k = i*dk - kmax, |k| = sqrt of the float
+ * sum of squares, W = 3.*(sin(kR) - kR*cos(kR))/pow(kR,3) with its
+ * cancellation at small kR), for runs that compare against the reference's
+ * output.  Default off: the default window is accurate to the float rounding
+ * of its argument at every kR.  Applies to the forward and smoothing passes;
+ * the adjoint keeps the accurate window. */
+#define PRC_FLAG_FAITHFUL_WINDOW 4
 
 #define PRC_NHISTORY      100000 /* allvars_d2z.h:1 */
 #define PRC_ARGMAX_NONE   255    /* argmax value of a cell never updated      */
@@ -141,8 +149,9 @@ int prc_d2z_create(const prc_d2z_desc* desc, prc_d2z_ctx** out);
  * PRC_ARGMAX_NONE where never updated) and sigma_grid (n_radii doubles).
  * Replaces main_d2z.C:57-71 (delta/=DInit, forward R2C, delta2zreion()),
  * i.e. the zreion field before GetHistory/CorrectHistory.  zreion starts at 0
- * (allocate_d2z.C:464); a radius updates a cell iff its z is strictly larger
- * (delta2zreion_d2z.C:138). */
+ * (allocate_d2z.C:37); a radius updates a cell iff its z is strictly larger
+ * (delta2zreion_d2z.C:138).  Returns PRC_ERR_CUDA (outputs incomplete) if a
+ * kernel's bounded wait for a staging copy ran out; the context stays usable. */
 int prc_d2z_forward(prc_d2z_ctx* ctx, const float* delta_lin, int delta_on_device,
                     float* zreion, uint8_t* argmax, int out_on_device,
                     double* sigma_grid);
@@ -293,12 +302,25 @@ int prc_d2z_destroy(prc_d2z_ctx* ctx);
  * delta_lin, zreion and argmax (nullable) are device pointers, N^3 each, laid
  * out as for prc_d2z_forward, whose zreion/argmax it reproduces; the call
  * returns after the work on `stream` has finished.  The first call on a device
- * performs a one-time set-up (it looks up the array's device address), so make
- * it before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU race, so serialise them. */
+ * performs a one-time set-up (it looks up the arrays' device addresses and
+ * writes the twiddle tables of every supported N into the array), so make it
+ * before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU race, so serialise them.  Like prc_d2z_forward it returns
+ * PRC_ERR_CUDA if a kernel's bounded wait for a staging copy ran out (the
+ * error word it reads for that is a second static array of one int, cleared
+ * by every call). */
 int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const double* radii_mpc,
                            const double* barrier_b, double barrier_a, double growth_init,
                            const float* delta_lin, float* zreion, uint8_t* argmax, void* stream);
+
+/* Test hook for the failure path of the bounded waits (no counterpart in the
+ * reference).  The next `calls` calls of prc_d2z_forward or
+ * prc_d2z_forward_static run their first sweep with one staging copy of the
+ * inverse z pass withheld (grids whose z pass stages lines by bulk copy:
+ * every N >= 32 except 48): the waiting CTA gives up after a
+ * short bounded wait with no copy in flight, the call returns PRC_ERR_CUDA
+ * and the next call runs normally.  0 cancels; process-wide. */
+int prc_d2z_test_withhold_copy(int calls);
 
 const char* prc_last_error(void);
 

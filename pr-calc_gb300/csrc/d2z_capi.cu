@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "../../include/prc_d2z.h"
@@ -27,6 +28,17 @@ namespace prc {
 PRC_DECL(8) PRC_DECL(12) PRC_DECL(16) PRC_DECL(24) PRC_DECL(32) PRC_DECL(48) PRC_DECL(64)
 PRC_DECL(96) PRC_DECL(128) PRC_DECL(192) PRC_DECL(256) PRC_DECL(512) PRC_DECL(1024)
 #undef PRC_DECL
+
+// Test hook (prc_d2z_test_withhold_copy): how many forward calls still run
+// their first sweep with one staging copy withheld.
+std::atomic<int> g_withhold{0};
+
+bool take_withhold() {
+  int v = g_withhold.load();
+  while (v > 0 && !g_withhold.compare_exchange_weak(v, v - 1)) {
+  }
+  return v > 0;
+}
 
 const KernelSet* kernel_set(int N) {
   switch (N) {
@@ -354,8 +366,10 @@ TileSeg qseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool transpose
 void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb = 1, int r0 = 0, int first = 0) {
   TileArgs a;
   memset(&a, 0, sizeof(a));
+  const bool faithful = mode == TM_WIN && (c->flags & PRC_FLAG_FAITHFUL_WINDOW);
+  const int wv = faithful ? 0 : c->win_var;  // the faithful window runs on variant 0's tiles
   if (mode == TM_WIN || mode == TM_ACC) {  // these passes may use narrower tiles
-    const int tw = mode == TM_WIN ? c->ksl.tile_w_winv[c->win_var] : c->ksl.tile_w_acc;
+    const int tw = mode == TM_WIN ? c->ksl.tile_w_winv[wv] : c->ksl.tile_w_acc;
     s0.tpo = (s0.nyq ? c->N : c->H) / tw;
     s1.tpo = (s1.nyq ? c->N : c->H) / tw;
   }
@@ -365,11 +379,21 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
   a.tw = c->tw;
   a.nb = nb;
   a.first = first;
-  a.win_var = c->win_var;
-  if (mode == TM_WIN || mode == TM_ACC)
+  a.win_var = wv;
+  if (faithful) {
+    // delta2zreion_d2z.C:41,43: dk = 2.*M_PI/BoxSize and kmax = dk*N in float;
+    // the window then takes the float radius itself
+    a.faithful = 1;
+    a.dk = (float)(2.0 * M_PI / (double)(float)c->box);
+    a.kmax = a.dk * (float)c->N;
+    for (int b = 0; b < nb; ++b) a.kr[b] = (float)c->R[r0 + b];
+  } else if (mode == TM_WIN || mode == TM_ACC) {
     for (int b = 0; b < nb; ++b) a.kr[b] = c->kr[r0 + b];
+  }
   const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
-  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc : (mode == TM_WIN) ? c->ksl.occ_winv[c->win_var] : c->ksl.occ_tile;
+  const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc
+                : faithful         ? c->ksl.occ_win_faithful
+                : (mode == TM_WIN) ? c->ksl.occ_winv[wv] : c->ksl.occ_tile;
   dim3 grid(grid_for(tiles, 1, occ, c->sms), gy, 1);
   const int kind = mode == TM_FWD ? PRC_KIND_COL_FWD
                  : mode == TM_INV ? PRC_KIND_COL_INV
@@ -417,7 +441,7 @@ void forward_r2c(prc_d2z_ctx* c, const float* d_delta, double divisor) {
 // The running max lives in d_z / d_am; the last sweep writes the final values
 // to z_out / am_out (default: d_z / d_am), which may be mapped host memory.
 void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, float* z_out = nullptr,
-                    uint8_t* am_out = nullptr) {
+                    uint8_t* am_out = nullptr, bool withhold = false) {
   const int N = c->N, H = c->H;
   const long long NN = c->NN;
   for (int r0 = 0; r0 < c->nr; r0 += c->B) {
@@ -434,6 +458,7 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, floa
     sa.argmax_out = d_am ? ((last && am_out) ? am_out : d_am) : nullptr;
     sa.sig_acc = sig;
     sa.err = c->err;
+    sa.withhold = (withhold && r0 == 0) ? 1 : 0;
     sa.nb = nb;
     sa.r0 = r0;
     sa.first = (r0 == 0);
@@ -500,6 +525,12 @@ void batch_enqueue(prc_d2z_batch* b, const float* const* delta, float* const* zr
 extern "C" {
 
 int prc_d2z_supported(int N) { return kernel_set(N) != nullptr ? 1 : 0; }
+
+int prc_d2z_test_withhold_copy(int calls) {
+  if (calls < 0) return prc_fail(PRC_ERR_INVALID, "prc_d2z_test_withhold_copy: calls must be >= 0");
+  g_withhold.store(calls);
+  return PRC_OK;
+}
 
 int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
   if (!d || !out) return prc_fail(PRC_ERR_INVALID, "prc_d2z_create: null argument");
@@ -675,7 +706,7 @@ int prc_d2z_forward(prc_d2z_ctx* c, const float* delta_lin, int delta_on_device,
   PRC_CU(cudaEventRecord(c->ev[0], c->st), "event");
   forward_r2c(c, d_delta, c->dinit);
   PRC_CU(cudaEventRecord(c->ev[1], c->st), "event");
-  enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr, z_final, am_final);
+  enqueue_sweeps(c, d_z, d_am, want_sig ? c->sig : nullptr, z_final, am_final, take_withhold());
   PRC_CU(cudaGetLastError(), "kernel launch");
   PRC_CU(cudaEventRecord(c->ev[2], c->st), "event");
   if (!out_on_device) {

@@ -117,6 +117,10 @@ template <> struct WinVar<256, 1> { static constexpr bool on = true; static cons
 template <> struct WinVar<256, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
 template <> struct WinVar<512, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
 template <> struct WinVar<512, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+// The faithful float window (PRC_FLAG_FAITHFUL_WINDOW) on variant 0's tiles
+// and plan: a launch code beside the variants, never chosen by the autotuner.
+constexpr int kWinFaithful = 7;
+template <int N> struct WinVar<N, kWinFaithful> : WinVar<N, 0> {};
 
 // Tile width and plan of a mode: the window pass uses its variant V, and the
 // accumulate mode uses variant 0 of the window pass when the plain plan holds
@@ -261,6 +265,8 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       gstore(w, w.sg.out + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
+    // FW: the reference's float window, every row evaluated on its own
+    constexpr bool FW = (V == kWinFaithful);
     float2 raw[E];
     int ti = blockIdx.x;
     if (ti < tiles) {
@@ -269,11 +275,23 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     }
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
-      float kq[EH + 1];
-      kmag(w, kq);
+      float kq[FW ? E : EH + 1];
+      if constexpr (FW) {
+        const int col = w.tc * T + c;
+        const int iy = w.sg.nyq ? col : w.outer, iz = w.sg.nyq ? H : col;
+#pragma unroll
+        for (int m = 0; m < E; ++m) kq[m] = rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax);
+      } else {
+        kmag(w, kq);
+      }
       auto radius = [&](int b, bool last) {
         float wv[E];
-        wvals(kq, s_kr[b], wv);
+        if constexpr (FW) {
+#pragma unroll
+          for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], s_kr[b]);
+        } else {
+          wvals(kq, s_kr[b], wv);
+        }
         float2 v[E];
 #pragma unroll
         for (int m = 0; m < E; ++m) v[m] = cscale(raw[m], wv[m]);

@@ -24,6 +24,7 @@ struct KernelSet {
   size_t tile_smem, line_smem;  // dynamic shared memory bytes
   // resident CTAs per SM (filled by init)
   int occ_tile, occ_tile_win, occ_tile_acc, occ_r2c, occ_c2r, occ_c2r_plain, occ_adj_z;
+  int occ_win_faithful;         // the window pass with the reference's float window
   cudaError_t (*init)(KernelSet*);
   void (*r2c_z)(const KernelSet&, int grid, cudaStream_t, const float* delta, float dinit,
                 float2* S, float2* Qt, const float2* tw);
@@ -36,5 +37,9 @@ struct KernelSet {
 
 // nullptr when N has no compiled plan
 const KernelSet* kernel_set(int N);
+
+// true (and one fewer pending) when prc_d2z_test_withhold_copy asked for a
+// withheld staging copy in the next forward call
+bool take_withhold();
 
 }  // namespace prc

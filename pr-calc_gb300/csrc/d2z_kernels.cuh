@@ -113,7 +113,9 @@ struct TileArgs {
   const float2* tw;        // N-entry table e^{+2 pi i k/N}
   int nb, first;
   int win_var;             // window-pass variant (host-side launch choice)
-  float kr[kMaxBatch];     // dk * R_b
+  int faithful;            // window pass: the reference's float window (kr holds R_b)
+  float dk, kmax;          // faithful window: dk = 2 pi / box and kmax = dk * N, in float
+  float kr[kMaxBatch];     // dk * R_b (faithful window: R_b)
 };
 
 struct SweepArgs {
@@ -126,6 +128,8 @@ struct SweepArgs {
   uint8_t* argmax_out;  // likewise for the argmax (null when argmax is null)
   double* sig_acc;      // per-radius sum of x^2 (raw C2R units) or null
   int* err;             // set to 1 when a copy wait ran out (null: not reported)
+  int withhold;         // test hook: CTA 0 never issues its first staging copy, so
+                        // that its bounded wait runs out (then after kWithheldPolls)
   int nb;               // radii in this sweep
   int r0;               // global index of the first radius
   int first;            // first sweep: zreion/argmax not read
@@ -175,6 +179,36 @@ __device__ __forceinline__ float tophat(float x) { return x < 1.0f ? tophat_smal
 
 __device__ __forceinline__ float window_of(int m2, float kr) {
   return (m2 == 0) ? 0.f : tophat(sqrtf((float)m2) * kr);
+}
+
+// The reference's own float window, operation by operation
+// (delta2zreion_d2z.C:41-43,59-82), for parity runs (PRC_FLAG_FAITHFUL_WINDOW):
+// k = i*dk, minus kmax = dk*N for i >= N/2 (the Nyquist index too); |k| =
+// sqrt((kx^2 + ky^2) + kz^2) in float; W = 3.*(sin(kR) - kR*cos(kR))/pow(kR, 3)
+// with float sine and cosine, the quotient in double (pow(kR, 3) is the
+// correctly rounded double product, as kR*kR is exact), rounded to float.
+// Every step is rounded as written (no contraction into FMAs), so the
+// cancellation of sin x - x cos x at small x is the reference's.  The float
+// sine and cosine are the correctly rounded ones (the double functions
+// rounded to float): the reference takes them from its C library, whose
+// sinf/cosf may differ from those by an ulp (glibc 2.39: about 1% of
+// arguments), so there is no bit-exact target; the cancellation amplifies such
+// an ulp by about 3/x^2.
+__device__ __forceinline__ float kfaithful(int i, int n, float dk, float kmax) {
+  const float k = __fmul_rn((float)i, dk);
+  return (i >= n / 2) ? __fsub_rn(k, kmax) : k;
+}
+__device__ __forceinline__ float rk_faithful(int ix, int iy, int iz, int n, float dk, float kmax) {
+  const float kx = kfaithful(ix, n, dk, kmax), ky = kfaithful(iy, n, dk, kmax), kz = kfaithful(iz, n, dk, kmax);
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz)));
+}
+__device__ __forceinline__ float window_faithful(float rk, float R) {
+  if (rk == 0.f) return 0.f;
+  const float x = __fmul_rn(rk, R);
+  const double xd = (double)x;
+  const float sx = __double2float_rn(sin(xd)), cx = __double2float_rn(cos(xd));
+  const float num = __fsub_rn(sx, __fmul_rn(x, cx));
+  return __double2float_rn(__ddiv_rn(__dmul_rn(3.0, (double)num), __dmul_rn(__dmul_rn(xd, xd), xd)));
 }
 
 __device__ __forceinline__ void load_tw(float2* tw_s, const float2* tw, int n) {
@@ -436,7 +470,13 @@ __global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_A
     const int c = w.tc * T + g;
     const int syz = w.sg.nyq ? fsq(c, N) + H * H : fsq(w.outer, N) + c * c;
     constexpr int EH = E / 2;
-    if constexpr (G <= 32) {
+    if (a.faithful) {
+      // every row on its own: rows ix and N - ix need not round alike here
+      const int iy = w.sg.nyq ? c : w.outer, iz = w.sg.nyq ? H : c;
+#pragma unroll
+      for (int m = 0; m < E; ++m)
+        v[m] = cscale(v[m], window_faithful(rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax), kr));
+    } else if constexpr (G <= 32) {
       float wv[EH + 1];
 #pragma unroll
       for (int m = 0; m <= EH; ++m) {

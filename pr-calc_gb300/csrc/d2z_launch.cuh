@@ -20,6 +20,9 @@ template <int N> struct ColLaunch<N, false> {
   static constexpr size_t TS = (size_t)TT::smem_f2 * sizeof(float2);    // one tile
   static constexpr size_t TS2 = (size_t)TT::smem2_f2 * sizeof(float2);  // two tiles (TM_WIN)
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_tile<N, MODE>); }
+  static void* faithful_fn() { return reinterpret_cast<void*>(&k_tile<N, TM_WIN>); }
+  static constexpr size_t FS = TS2;
+  static constexpr int FTHREADS = THREADS;
   static size_t bytes(int mode) { return mode == TM_WIN ? TS2 : TS; }
   static int threads(int) { return THREADS; }
   static constexpr int T_ACC = T;
@@ -80,7 +83,15 @@ template <int N> struct ColLaunch<N, true> {
     win_info<0>(v, &n, f ? f : &f0, thr ? thr : &t0, by ? by : &b0, tw ? tw : &w0);
     return n;
   }
+  using WF = typename ColK<N, TM_WIN, kWinFaithful>::type;
+  static void* faithful_fn() { return reinterpret_cast<void*>(&k_col<N, TM_WIN, kWinFaithful>); }
+  static constexpr size_t FS = (size_t)WF::smem_f2 * sizeof(float2);
+  static constexpr int FTHREADS = WF::THREADS;
   template <int V> static void launch_win(int v, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    if (V == 0 && a.faithful) {
+      k_col<N, TM_WIN, kWinFaithful><<<grid, FTHREADS, FS, st>>>(a);
+      return;
+    }
     if constexpr (V < kWinVariants) {
       if constexpr (Win<V>::on) {
         if (v == V) {
@@ -162,6 +173,8 @@ template <int N> struct Launchers {
     }
     ks->occ_tile_win = ks->occ_winv[0];
     ks->tile_w_win = ks->tile_w_winv[0];
+    if ((e = smem(CL::faithful_fn(), CL::FS)) != cudaSuccess) return e;
+    if ((e = occ(&ks->occ_win_faithful, CL::faithful_fn(), CL::FTHREADS, CL::FS)) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
     for (int i = 0; i < CR::NFN; ++i)
       if ((e = smem(CR::fn(i), CR::BYTES)) != cudaSuccess) return e;

@@ -97,13 +97,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int li
   return false;
 }
 constexpr int kWaitPolls = 1 << 22;  // each poll may suspend; far beyond any copy
+constexpr int kWithheldPolls = 256;  // wait limit of a CTA whose copy the test hook withheld
 
 // Steps (line group s, radius b) run in order; the input of the next step is
 // copied into the other staging buffer while the current one is transformed:
 // the NG lines of a step are one contiguous block of the slot, fetched by one
 // TMA bulk copy (cp.async.bulk) issued by thread 0 and completing on that
 // buffer's mbarrier; the NG Nyquist values come with 8-byte cp.async.  A wait
-// that runs out of polls stops the whole CTA and sets *a.err.
+// that runs out of polls stops the whole CTA and sets *a.err; before the CTA
+// exits, thread 0 (which issued the copy) waits once more, again bounded, for
+// that copy to land, so that no bulk copy is left writing into the shared
+// memory of a CTA that has gone (the 8-byte copies end at cp_async_wait).
+// a.withhold (a test hook) makes CTA 0 skip its first bulk copy, so that its
+// first wait runs out for real, with nothing in flight.
 // AM: argmax wanted (a.argmax != null); its bytes are packed four to a register.
 // SIG: per-radius sums of x^2 wanted (a.sig_acc != null).
 template <int N, bool AM, bool SIG>
@@ -142,11 +148,13 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   __syncthreads();
 
   // copies of step (line group lg of this CTA, radius b) into staging buffer bi
+  const bool withheld = a.withhold && blockIdx.x == 0;
   auto issue = [&](int lg, int b, int bi) {
     if (lg < nsteps_l) {
       const long long l0 = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG;
       const float2* slot = a.slots + (long long)b * a.slot_stride;
-      if (threadIdx.x == 0) bulk_load(stage + bi * STG, slot + l0 * H, STG * 8, &s_bar[bi]);
+      if (threadIdx.x == 0 && !(withheld && lg == 0 && b == 0))
+        bulk_load(stage + bi * STG, slot + l0 * H, STG * 8, &s_bar[bi]);
       if (t == 0) {
         const long long l = l0 + g;
         const int ix = (int)(l / N), iy = (int)(l - (l / N) * N);
@@ -188,11 +196,17 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
       }
     }
     // step i uses buffer bi for the (i >> 1)-th time: barrier phase (i >> 1) & 1
-    const bool late = !mbar_wait(&s_bar[bi], (unsigned)((i >> 1) & 1), kWaitPolls);
+    const unsigned phase = (unsigned)((i >> 1) & 1);
+    const bool late = !mbar_wait(&s_bar[bi], phase, (withheld && i == 0) ? kWithheldPolls : kWaitPolls);
     cp_async_wait<0>();
     // step i staged for everyone; everyone is done reading buffer (i+1) & 1
     if (__syncthreads_or(late)) {
-      if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+      if (threadIdx.x == 0) {
+        if (a.err) atomicExch(a.err, 1);
+        // the copy this step waited for may still be landing: wait for it
+        // (bounded) before the CTA's shared memory is released
+        if (!(withheld && i == 0)) mbar_wait(&s_bar[bi], phase, kWaitPolls);
+      }
       break;
     }
     issue(lg_next, nb_next, bi ^ 1);

@@ -14,10 +14,13 @@
 // Limits and sharing: the array is sized for grids up to N = 64 (about
 // 2.2 MB).  All calls share it and it keeps the last call's contents, so two
 // calls whose work overlaps on the GPU (different streams, or different host
-// threads on one device) race on it; serialise them.  Nothing in it has to
-// start at zero: every call rewrites the twiddles, the spectrum and the slot
-// before reading them, and the first radius writes zreion and argmax without
-// reading them.
+// threads on one device) race on it; serialise them.  The twiddle tables of
+// every supported N are written once per device, at the first call; the
+// spectrum and the slot need not start at zero (every call writes them before
+// reading them, and the first radius writes zreion and argmax without reading
+// them).  The one word that must start at zero, the kernels' error word (a
+// second file-scope array), is cleared on the stream at the start of every
+// call and read back after the call's synchronisation.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -34,16 +37,67 @@ namespace {
 
 constexpr int kStaticMaxN = 64;
 constexpr long long kStaticSlotF2 = (long long)kStaticMaxN * kStaticMaxN * (kStaticMaxN / 2 + 2);
-// spectrum + one radius slot + twiddle table, in float2
-constexpr long long kStaticF2 = 2 * kStaticSlotF2 + kStaticMaxN;
+constexpr int kSmallN[7] = {8, 12, 16, 24, 32, 48, 64};
+constexpr int kTwAll = 8 + 12 + 16 + 24 + 32 + 48 + 64;  // one twiddle table per supported N
+// spectrum + one radius slot + the twiddle tables, in float2
+constexpr long long kStaticF2 = 2 * kStaticSlotF2 + kTwAll;
 
 static __device__ __align__(256) float2 g_static_scratch[kStaticF2];
+static __device__ __align__(256) int g_static_err[1];  // set by a z-pass CTA whose copy wait ran out
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 float2* g_scratch_ptr[kMaxDevices] = {};      // device address of g_static_scratch, per device
-prc::KernelSet g_ks[kMaxDevices][8];          // per device, per supported small N
-bool g_ks_ready[kMaxDevices][8] = {};
+int* g_err_ptr[kMaxDevices] = {};             // device address of g_static_err, per device
+prc::KernelSet g_ks[kMaxDevices][7];          // per device, per supported small N
+bool g_ready[kMaxDevices] = {};
+
+// offset of grid side N's twiddle table after the spectrum and the slot
+int tw_offset(int si) {
+  int o = 0;
+  for (int i = 0; i < si; ++i) o += kSmallN[i];
+  return o;
+}
+
+// Per-device set-up, with that device current: the device addresses of the
+// two arrays (their host-side names are only stand-ins), every small N's
+// twiddle table e^{+2 pi i k/N} (built in FP64, one synchronous copy) and the
+// kernels' shared-memory limits.
+int setup_device(int dev) {
+  using namespace prc;
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess || !p)
+    return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  void* q = nullptr;
+  e = cudaGetSymbolAddress(&q, g_static_err);
+  if (e != cudaSuccess || !q)
+    return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  float2 htw[kTwAll];
+  for (int si = 0; si < 7; ++si) {
+    const int N = kSmallN[si];
+    for (int k = 0; k < N; ++k) {
+      const double ang = 2.0 * M_PI * (double)k / (double)N;
+      htw[tw_offset(si) + k] = make_float2((float)cos(ang), (float)sin(ang));
+    }
+  }
+  float2* tw = static_cast<float2*>(p) + 2 * kStaticSlotF2;
+  e = cudaMemcpy(tw, htw, sizeof(htw), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess)
+    return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: twiddle tables: %s", cudaGetErrorString(e));
+  for (int si = 0; si < 7; ++si) {
+    const KernelSet* ks = kernel_set(kSmallN[si]);
+    if (!ks) return prc_fail(PRC_ERR_UNSUPPORTED, "prc_d2z_forward_static: no FFT plan for N=%d", kSmallN[si]);
+    g_ks[dev][si] = *ks;
+    e = ks->init(&g_ks[dev][si]);
+    if (e != cudaSuccess)
+      return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: kernel set-up: %s", cudaGetErrorString(e));
+  }
+  g_scratch_ptr[dev] = static_cast<float2*>(p);
+  g_err_ptr[dev] = static_cast<int*>(q);
+  g_ready[dev] = true;
+  return PRC_OK;
+}
 
 int small_index(int N) {
   switch (N) {
@@ -89,28 +143,14 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
   if (e == cudaSuccess && (dev < 0 || dev >= kMaxDevices)) e = cudaErrorInvalidDevice;
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: device query: %s", cudaGetErrorString(e));
-  // Set-up, once per device and grid size, with that device current: the
-  // device address of the static array (its host-side name is only a
-  // stand-in) and the kernels' shared-memory limits.  This happens inside
-  // the first call on a device, so make that first call before any stream
-  // capture begins.
+  // Set-up, once per device, with that device current (setup_device).  It
+  // happens inside the first call on a device, so make that first call before
+  // any stream capture begins.
   {
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_static_scratch);
-      if (e != cudaSuccess || !p)
-        return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-      g_scratch_ptr[dev] = static_cast<float2*>(p);
-    }
-    if (!g_ks_ready[dev][si]) {
-      const KernelSet* ks = kernel_set(N);
-      if (!ks) return prc_fail(PRC_ERR_UNSUPPORTED, "prc_d2z_forward_static: no FFT plan for N=%d", N);
-      g_ks[dev][si] = *ks;
-      e = ks->init(&g_ks[dev][si]);
-      if (e != cudaSuccess)
-        return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: kernel set-up: %s", cudaGetErrorString(e));
-      g_ks_ready[dev][si] = true;
+    if (!g_ready[dev]) {
+      const int st = setup_device(dev);
+      if (st != PRC_OK) return st;
     }
   }
   const KernelSet& ks = g_ks[dev][si];
@@ -119,16 +159,11 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
   const long long NN = (long long)N * N, slot_f2 = NN * (H + 2);
   float2* spec = g_scratch_ptr[dev];
   float2* slot = spec + slot_f2;
-  float2* tw = slot + slot_f2;
-
-  // twiddles e^{+2 pi i k/N} in FP64, copied from the stack into the array
-  float2 htw[kStaticMaxN];
-  for (int k = 0; k < N; ++k) {
-    const double ang = 2.0 * M_PI * (double)k / (double)N;
-    htw[k] = make_float2((float)cos(ang), (float)sin(ang));
-  }
-  e = cudaMemcpyAsync(tw, htw, sizeof(float2) * N, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: twiddles: %s", cudaGetErrorString(e));
+  const float2* tw = spec + 2 * kStaticSlotF2 + tw_offset(si);
+  int* d_err = g_err_ptr[dev];
+  e = cudaMemsetAsync(d_err, 0, sizeof(int), st);
+  if (e != cudaSuccess) return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: clear error word: %s", cudaGetErrorString(e));
+  const bool withhold = take_withhold();
 
   auto mseg = [&](const float2* in, float2* out, bool xpass) {
     TileSeg s;
@@ -194,6 +229,8 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     sa.zreion_out = d_zreion;
     sa.argmax_out = d_argmax;
     sa.sig_acc = nullptr;
+    sa.err = d_err;
+    sa.withhold = (withhold && r == 0) ? 1 : 0;
     sa.nb = 1;
     sa.r0 = r;
     sa.first = (r == 0);
@@ -201,8 +238,12 @@ extern "C" int prc_d2z_forward_static(int N, int n_radii, double box_mpc, const 
     sa.cb[0] = (float)(barrier_a * barrier_b[r] - 1.0);
     ks.c2r_z(ks, grid_of((N * N + ks.c2r_lines - 1) / ks.c2r_lines, ks.occ_c2r, sms), st, sa);
   }
+  int h_err = 0;
   e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: %s", cudaGetErrorString(e));
+  if (h_err)
+    return prc_fail(PRC_ERR_CUDA, "prc_d2z_forward_static: a staging copy did not complete within the wait limit");
   return PRC_OK;
 }

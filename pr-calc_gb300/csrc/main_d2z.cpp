@@ -351,7 +351,10 @@ int main(int argc, char* argv[]) {
     std::vector<float> rb((size_t)n3);
     for (long long i = 0; i < n3; ++i) rb[i] = argmax[i] == PRC_ARGMAX_NONE ? 0.f : (float)R[argmax[i]];
     std::string rname = std::string(CL.Basename) + ".rbubble";
-    write_all(rname.c_str(), rb.data(), sizeof(float) * n3);
+    if (!write_all(rname.c_str(), rb.data(), sizeof(float) * n3)) {
+      printf("\n cannot write %s\n", rname.c_str());
+      return 1;
+    }
     printf("\n Bubble sizes written...");
   }
   // GetHistory of the corrected field, tau (main_d2z.C:97-98), WriteHistory (:101)

@@ -243,7 +243,8 @@ class Delta2Zreion:
     """One box on the GPU (prc_d2z_create .. prc_d2z_destroy)."""
 
     def __init__(self, N: int, box_mpc: float, radii_mpc, barrier_b, barrier_a: float, growth_init: float = 1.0,
-                 radius_batch: int = 0, argmax: bool = True, sigma_grid: bool = False, stream=None):
+                 radius_batch: int = 0, argmax: bool = True, sigma_grid: bool = False, stream=None,
+                 faithful_window: bool = False):
         L = load()
         self.N = int(N)
         self.n3 = self.N ** 3
@@ -261,7 +262,8 @@ class Delta2Zreion:
         d.barrier_a = self.barrier_a
         d.growth_init = self.growth_init
         d.radius_batch = int(radius_batch)
-        d.flags = (PRC_FLAG_ARGMAX if argmax else 0) | (PRC_FLAG_SIGMA_GRID if sigma_grid else 0)
+        d.flags = ((PRC_FLAG_ARGMAX if argmax else 0) | (PRC_FLAG_SIGMA_GRID if sigma_grid else 0)
+                   | (_lib.PRC_FLAG_FAITHFUL_WINDOW if faithful_window else 0))
         d.stream = ctypes.c_void_p(int(stream)) if stream is not None else None
         self._ctx = ctypes.c_void_p()
         check(L.prc_d2z_create(ctypes.byref(d), ctypes.byref(self._ctx)))

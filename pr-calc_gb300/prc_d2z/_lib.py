@@ -19,6 +19,7 @@ PRC_ERR_IO = -5
 PRC_ERR_NUMERIC = -6
 PRC_FLAG_ARGMAX = 1
 PRC_FLAG_SIGMA_GRID = 2
+PRC_FLAG_FAITHFUL_WINDOW = 4
 PRC_NHISTORY = 100000
 PRC_ARGMAX_NONE = 255
 PRC_MAX_RADII = 254
@@ -36,7 +37,7 @@ EXPORTS = [
     "prc_chistory", "prc_zvz", "prc_d2z_correct", "prc_d2z_batch_create", "prc_d2z_batch_forward",
     "prc_d2z_batch_launches", "prc_d2z_batch_destroy", "prc_d2z_set_barrier",
     "prc_white_noise", "prc_d2z_gaussian_field", "prc_d2z_win_variants", "prc_d2z_tune",
-    "prc_d2z_batch_tune", "prc_last_error",
+    "prc_d2z_batch_tune", "prc_d2z_test_withhold_copy", "prc_last_error",
 ]
 
 
@@ -145,6 +146,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.prc_d2z_batch_tune.argtypes = [vp, c_int, c_int, c_int]
     L.prc_white_noise.argtypes = [vp, ctypes.c_longlong, ctypes.c_uint, vp]
     L.prc_d2z_gaussian_field.argtypes = [vp, ctypes.c_uint, vp, c_int, vp, c_int]
+    L.prc_d2z_test_withhold_copy.argtypes = [c_int]
     for name in EXPORTS:
         if name in ("prc_f2f_free",):
             continue

@@ -52,7 +52,9 @@ def test_oracle_reproduces_fixture(name):
 @pytest.mark.parametrize("name", CASES)
 def test_host_tables_match_fixture(name):
     """The C++ host tables (prc_compute_tables) give the fixture's radii and,
-    within the reference's 1e-4 bracket of erfc^-1, its barrier offsets."""
+    within the reference's 1e-4 bracket of erfc^-1 (the fixtures hold the
+    exact root), its barrier offsets; tests/test_cpu_tables.py pins every
+    other factor of B_r to 1e-6."""
     g = _load(name)
     N = int(g["N"])
     p = prc_d2z.Parameters(N=N, Nscales=len(g["radii_mpc"]), BoxSize=float(g["box_hmpc"]), Rmin=2.0)
@@ -64,4 +66,4 @@ def test_host_tables_match_fixture(name):
     np.testing.assert_allclose(t.DInit, float(g["dinit"]), rtol=1e-7)
     ok = np.isfinite(g["barrier_b"])
     assert np.array_equal(np.isfinite(t.barrier_b), ok)
-    np.testing.assert_allclose(t.barrier_b[ok], g["barrier_b"][ok], rtol=2e-4)
+    np.testing.assert_allclose(t.barrier_b[ok], g["barrier_b"][ok], rtol=1e-4)

@@ -1,0 +1,177 @@
+"""GPU parity on the workloads' own parameters and on the parts of the chain
+the other tests leave at their defaults: the 128^3 plain configuration exactly
+(200 Mpc/h, 32 radii from 2 cells to 60 Mpc/h, zeta 82.44, M_min 1e9 Msun/h,
+seed 1), a start redshift zInit = 6 (D_init != 1 through the forward R2C and
+the adjoint, main_d2z.C:57-59), and the faithful float window
+(PRC_FLAG_FAITHFUL_WINDOW, delta2zreion_d2z.C:41-43,59-82)."""
+import math
+
+import numpy as np
+import pytest
+
+import prc_d2z
+from oracle import d2z_ref as orc
+from prc_d2z import fields
+
+pytestmark = pytest.mark.gpu
+H_ = 0.68
+
+
+def _eps_z(A, dmax, z):
+    return A * 1e-5 * dmax + 2 * np.spacing(np.abs(z).astype(np.float32)).astype(np.float64)
+
+
+def _c1():
+    """The 128^3 plain workload: 200 Mpc/h box, 32 radii from 2 cells to
+    60 Mpc/h, zeta 82.44 (x_i(z=8) = 0.5 at seed 1), M_min = 1e9 Msun/h."""
+    p = prc_d2z.Parameters(N=128, Nscales=32, BoxSize=200.0, Rmin=2.0)
+    cl = prc_d2z.CLParameters(Rmax=60.0, zeta=82.44, M_min=1e9 / H_)
+    return p, cl, fields.gaussian_field(128, 200.0, seed=1), prc_d2z.compute_tables(p, cl), \
+        float(np.float32(200.0) / np.float32(H_))
+
+
+def _check_rule(z, am, zs, dmax, A, tight=1.0):
+    """zreion within eps_z (times `tight`) and argmax identical on every cell
+    whose FP64 top-two margin exceeds eps_z; returns (near-barrier fraction,
+    largest |dz| on clear cells, largest allowed)."""
+    best, rbest, gap = orc.margins(zs)
+    zo = np.where(best > 0, best, 0.0)
+    amo = np.where(best > 0, rbest, 255)
+    eps = _eps_z(A, dmax, zo)
+    clear = gap > eps
+    dz = np.abs(z.astype(np.float64) - zo)
+    assert np.all(dz[clear] <= tight * eps[clear]), (float(dz[clear].max()), float((tight * eps[clear]).min()))
+    assert np.array_equal(am[clear], amo[clear].astype(np.uint8))
+    assert np.all(dz <= eps + np.maximum(gap, 0) + 1e-6)
+    return 1.0 - clear.mean(), float(dz[clear].max()), float(eps[clear].min())
+
+
+@pytest.mark.parametrize("faithful", [False, True])
+def test_c1_against_full_fp32_oracle(faithful):
+    """The 128^3 x 32 workload against the whole fp32 oracle chain
+    (orc.d2z): zreion within eps_z / 10 and argmax identical on the cells
+    whose fp32-oracle top-two margin exceeds eps_z / 10; the FP64 rule on
+    every clear cell; sigma_grid to 1e-5.  The near-barrier fraction is
+    printed."""
+    p, cl, delta, t, box_mpc = _c1()
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl, sigma_grid=True, faithful_window=faithful) as ctx:
+        z, am, sig = ctx.forward(delta, want_sigma_grid=True)
+    args = (box_mpc, t.radii_mpc, t.barrier_a, t.barrier_b, t.DInit)
+    zo, amo, sigo = orc.d2z(delta, *args, mode="fp32")
+    np.testing.assert_allclose(sig, sigo, rtol=1e-5)
+    zs32, dmax = orc.z_stack(delta, *args, mode="fp32")
+    _, _, gap32 = orc.margins(zs32)
+    eps10 = _eps_z(t.barrier_a, dmax, zo) / 10
+    clear = gap32 > eps10
+    dz = np.abs(z.astype(np.float64) - zo.astype(np.float64))
+    assert np.all(dz[clear] <= eps10[clear]), float(dz[clear].max())
+    assert np.array_equal(am[clear], amo[clear])
+    zs64, dmax64 = orc.z_stack(delta.astype(np.float64), *args, mode="fp64")
+    frac, worst, _ = _check_rule(z, am, zs64, dmax64, t.barrier_a)
+    assert frac < 0.02, frac
+    print(f"c1 faithful={faithful}: near-barrier {frac:.4%}, largest |dz| on clear cells {worst:.2e}, "
+          f"fp32-oracle agreement {np.mean(am == amo):.6f}")
+
+
+def test_zinit6_forward_and_adjoint():
+    """zInit = 6: delta_lin is divided by D(6) = 0.182 in the forward R2C
+    (main_d2z.C:57-59) and the adjoint carries the 1/D; forward against the
+    FP64 rule, adjoint against the FP64 adjoint with the same D."""
+    N = 64
+    box = 96.0
+    p = prc_d2z.Parameters(N=N, Nscales=12, BoxSize=box, zInit=6.0)
+    cl = prc_d2z.CLParameters(Rmax=30.0, zeta=30.0, M_min=1.47e9)
+    t = prc_d2z.compute_tables(p, cl)
+    assert abs(t.DInit - 0.18199588) < 1e-7
+    box_mpc = float(np.float32(box) / np.float32(H_))
+    # a field at z = 6 (the z = 0 field scaled by D(6)), so that zreion is
+    # the same physical field as at zInit = 0
+    delta = (fields.gaussian_field(N, box, seed=61) * np.float32(t.DInit)).astype(np.float32)
+    args = (box_mpc, t.radii_mpc, t.barrier_a, t.barrier_b, t.DInit)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl) as ctx:
+        z, am, _ = ctx.forward(delta)
+        g = np.random.default_rng(6).standard_normal(delta.shape).astype(np.float32)
+        dd, dB = ctx.backward(g, am)
+    zs, dmax = orc.z_stack(delta.astype(np.float64), *args, mode="fp64")
+    frac, _, _ = _check_rule(z, am, zs, dmax, t.barrier_a)
+    assert frac < 0.01, frac
+    assert (z > 0).mean() > 0.1
+    ref, dBref = orc.adjoint(g, am, box_mpc, t.radii_mpc, t.barrier_a, t.DInit)
+    rel = np.linalg.norm(dd - ref) / np.linalg.norm(ref)
+    assert rel < 1e-5, rel
+    np.testing.assert_allclose(dB, dBref, rtol=1e-5, atol=1e-9 * np.abs(dBref).max())
+    # the same field at zInit = 0 (delta / D) gives the same zreion within eps_z
+    p0 = prc_d2z.Parameters(N=N, Nscales=12, BoxSize=box, zInit=0.0)
+    t0 = prc_d2z.compute_tables(p0, cl)
+    with prc_d2z.Delta2Zreion.from_parameters(p0, cl) as ctx0:
+        z0, _, _ = ctx0.forward((delta / np.float32(t.DInit)).astype(np.float32))
+    eps = _eps_z(t.barrier_a, dmax, z0)
+    ok = np.abs(z.astype(np.float64) - z0) <= eps
+    assert ok.mean() > 0.99
+    assert np.array_equal(t0.barrier_b, t.barrier_b)
+
+
+def _faithful_w(f, N, box_mpc, R):
+    """The faithful window at integer frequency f = (i, j, k) of the half
+    spectrum, in numpy, with the correctly rounded float sine and cosine that
+    the kernel uses (the reference's own float/double steps otherwise)."""
+    f32, f64 = np.float32, np.float64
+    dk = f32(2 * math.pi / f64(f32(box_mpc)))
+    kmax = f32(dk * f32(N))
+
+    def kf(i):
+        k = f32(f32(i) * dk)
+        return f32(k - kmax) if i >= N // 2 else k
+
+    kx, ky, kz = (kf(i) for i in f)
+    rk = np.sqrt(f32(f32(f32(kx * kx) + f32(ky * ky)) + f32(kz * kz)), dtype=f32)
+    x = f32(rk * f32(R))
+    sx, cx = f32(math.sin(f64(x))), f32(math.cos(f64(x)))
+    num = f32(sx - f32(x * cx))
+    xd = f64(x)
+    return f32(3.0 * f64(num) / (xd * xd * xd)), float(x)
+
+
+def _exact_w(x):
+    if x < 1e-2:
+        return 1 - x * x / 10 + x ** 4 / 280
+    return 3 * (math.sin(x) - x * math.cos(x)) / x ** 3
+
+
+@pytest.mark.parametrize("N", [24, 32, 128, 512])
+def test_faithful_window_on_plane_waves(N):
+    """delta_lin = a plane wave at frequency f: delta_R / delta_lin is W(|k| R).
+    With the faithful flag the GPU's W equals the reference's float window
+    (here with correctly rounded sin/cos) to the float rounding of the
+    transforms, down to kR = 0.003 and 0.01 where that window is 2e-2 and
+    2.5e-4 away from the exact one; without it the GPU's W is the exact one
+    to the accuracy of its SFU sine and cosine.  24 runs the staged tile
+    kernel, 32/128/512 the column kernels (512: 8-column tiles)."""
+    import torch
+    box = 1.5 * N
+    box_mpc = float(np.float32(box) / np.float32(H_))
+    dk = 2 * math.pi / box_mpc
+    ar = torch.arange(N, device="cuda", dtype=torch.int64)
+    cases = [((1, 2, 3), 0.003), ((1, 2, 3), 0.01), ((1, 2, 3), 0.05), ((N - 1, 0, 1), 0.3),
+             ((2, N - 3, 5), 2.0), ((3, 1, 2), 7.0)]
+    for f, xt in cases:
+        kmag = dk * math.sqrt(sum(min(a, N - a) ** 2 for a in f))
+        R = float(np.float32(xt / kmag))
+        ph = (f[0] * ar[:, None, None] + f[1] * ar[None, :, None] + f[2] * ar[None, None, :]) % N
+        wave = torch.cos(2 * math.pi * ph.to(torch.float64) / N).to(torch.float32).contiguous()
+        del ph
+        w64 = wave.to(torch.float64)
+        got = {}
+        for faithful in (False, True):
+            with prc_d2z.Delta2Zreion(N, box_mpc, [R, 2 * R], [1.0, 1.0], 0.75, faithful_window=faithful) as ctx:
+                dR = ctx.smooth(wave, 0).to(torch.float64)
+            got[faithful] = float((dR * w64).sum() / (w64 * w64).sum())
+            del dR
+        wf, x = _faithful_w(f, N, box_mpc, R)
+        we = _exact_w(x)
+        tol = 5e-7 + 5e-7 * abs(we)
+        assert abs(got[True] - wf) <= tol, (f, x, got[True], float(wf), we)
+        assert abs(got[False] - we) <= 4 * tol, (f, x, got[False], we)
+        if x < 0.02:
+            # the faithful window's cancellation is what the flag reproduces
+            assert abs(float(wf) - we) > 100 * tol, (x, float(wf), we)

@@ -103,3 +103,46 @@ def test_executable_requires_fcoll_table(tmp_path):
     assert r.returncode != 0
     assert "fcoll_table.tab" in r.stdout
     assert not (tmp_path / "output" / "run.zreion").exists()
+
+
+def test_executable_records_bubble_sizes(tmp_path):
+    """RecordBubbleSizes 1: the executable writes <base>.rbubble, the radius
+    [Mpc] of each cell's winning scale (delta2zreion_d2z.C:117-120, written as
+    by WriteRbubbleFile, io_d2z.C:248-282: raw float32 N^3, file order), and 0
+    where no scale won (the reference leaves those cells unset).  It equals
+    R[argmax] of the forward call and of the fp32 oracle on clear cells."""
+    from oracle import d2z_ref as orc
+    exe = os.path.join(REPO, "pr-calc_gb300", "bin", "delta2zreion")
+    N, box = 32, 48.0
+    delta = fields.gaussian_field(N, box, seed=8)
+    delta.tofile(tmp_path / "delta")
+    smin = prc_d2z.compute_tables(prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box),
+                                  prc_d2z.CLParameters(Rmax=20.0, zeta=30.0, M_min=1.47e9)).sigma_min
+    z = np.linspace(0.0, 50.0, 2001)
+    with open(tmp_path / "fcoll_table.tab", "wb") as fh:
+        np.array([0.0, 50.0], np.float32).tofile(fh)
+        np.array([len(z)], np.int32).tofile(fh)
+        np.array([hr.fcoll(v, 0.31, 0.69, -1.0, smin) for v in z], np.float32).tofile(fh)
+    (tmp_path / "param.d2z").write_text(
+        "Omegam 0.31\nOmegal 0.69\nOmegab 0.049\nh 0.68\nns 0.965\nsigma8 0.81\nw -1\n"
+        f"BoxSize {box}\nN {N}\nzInit 0\nDeltaFile delta\nRmin 2\nNscales 10\nRecordBubbleSizes 1\n")
+    r = subprocess.run([exe, "param.d2z", "-f", "run", "-m", "1.47e9", "-z", "30", "-r", "20", "-v", "-e"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Bubble sizes written" in r.stdout
+    rb = np.fromfile(tmp_path / "output" / "run.rbubble", np.float32)
+    assert rb.size == N ** 3
+    rb = rb.reshape(N, N, N)
+    p = prc_d2z.Parameters(N=N, Nscales=10, BoxSize=box, RecordBubbleSizes=1)
+    cl = prc_d2z.CLParameters(Rmax=20.0, zeta=30.0, M_min=1.47e9)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl) as ctx:
+        _, am, _ = ctx.forward(delta)
+        t = ctx.tables
+    Rf = t.radii_mpc.astype(np.float32)
+    want = np.where(am == 255, np.float32(0), Rf[np.minimum(am, len(Rf) - 1)])
+    assert np.array_equal(rb, want)
+    assert (rb > 0).mean() > 0.05
+    box_mpc = float(np.float32(box) / np.float32(H_))
+    _, amo, _ = orc.d2z(delta, box_mpc, t.radii_mpc, t.barrier_a, t.barrier_b, t.DInit, mode="fp32")
+    wo = np.where(amo == 255, np.float32(0), Rf[np.minimum(amo, len(Rf) - 1)])
+    assert np.mean(rb == wo) > 0.999
