@@ -108,7 +108,7 @@ typedef struct {
   const double* barrier_b;        /* n_radii barrier offsets B_r (NaN: radius never wins) */
   double        barrier_a;        /* A in z = A*(delta_R + B_r) - 1             */
   double        growth_init;      /* D(zInit); delta_lin is divided by it (main_d2z.C:59) */
-  int           radius_batch;     /* radii per sweep, <= 32; 0 = 16 (8 for N >= 1024) */
+  int           radius_batch;     /* radii per sweep, <= 64; 0 = 16 (8 for N >= 1024) */
   int           flags;            /* PRC_FLAG_*                                 */
   void*         stream;           /* cudaStream_t; NULL = default stream        */
 } prc_d2z_desc;

@@ -57,7 +57,9 @@ template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<1
 // exchange buffer, no register prefetch -- 1-2% slower over the whole step.)
 template <> struct CCfg<1024> { static constexpr bool on = true; using P = Plan<16, 16, 16, 4>; static constexpr int T = 8, TWIN = 8; };
 
-template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK {
+// PPF: -1 two exchange buffers when they fit, 0 one; MINB_: resident CTAs per
+// SM the registers are sized for (0: by the CTA size).
+template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P, int PPF = -1, int MINB_ = 0> struct CK {
   using P = P_;
   static constexpr int H = N / 2, T = T_, E = P::E, G = N / E, THREADS = T * G;
   static_assert(PlanRun<P>::L == N, "column plan length");
@@ -68,10 +70,10 @@ template <int N, int T_ = CCfg<N>::T, class P_ = typename CCfg<N>::P> struct CK 
   static constexpr int BUF = N * T;                     // one exchange buffer
   // two exchange buffers (one barrier per exchange) when they fit in shared
   // memory, else one (two barriers per exchange: 1024 rows x 16 columns)
-  static constexpr bool PP = (TW + 2 * BUF) * 8 <= 200 * 1024;
+  static constexpr bool PP = PPF >= 0 ? PPF == 1 : (TW + 2 * BUF) * 8 <= 200 * 1024;
   static constexpr int smem_f2 = TW + (PP ? 2 : 1) * BUF;
   // resident CTAs per SM the register budget is sized for (E = 8: two 512-thread CTAs)
-  static constexpr int MINB = THREADS >= 512 ? (E <= 8 ? 2 : 1) : (THREADS >= 256 ? 2 : 4);
+  static constexpr int MINB = MINB_ > 0 ? MINB_ : THREADS >= 512 ? (E <= 8 ? 2 : 1) : (THREADS >= 256 ? 2 : 4);
 };
 
 // Two exchange buffers, column c: row p at (p ^ swz(p))*T + c.  swz is linear
@@ -105,18 +107,24 @@ struct CtaSync {
 
 // Window-pass variants (tile width, plan) the autotuner chooses among.
 // Variant 0 is the default (TWIN / PWIN); up to kWinVariants per grid size.
+// PPF / MINB as in CK.  (At N = 512, 8-column tiles re-read from L1 for every
+// radius instead of held in registers, in three 256-thread CTAs per SM with
+// one or two exchange buffers, measured 9.3-9.8 ms per 32-radius launch
+// against 5.05 ms for the register-held tile: at 80 registers the transform
+// spills, and the re-reads wait in its critical path.)
 constexpr int kWinVariants = 3;
-template <int N, int V> struct WinVar { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
-template <int N> struct WinVar<N, 0> {
+struct WinDef { static constexpr int PPF = -1, MINB = 0; };
+template <int N, int V> struct WinVar : WinDef { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
+template <int N> struct WinVar<N, 0> : WinDef {
   static constexpr bool on = CCfg<N>::on;
   static constexpr int T = CCfg<N>::TWIN;
   using P = typename WinPlan<CCfg<N>>::type;
 };
-template <> struct WinVar<128, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
-template <> struct WinVar<256, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<256, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
-template <> struct WinVar<512, 1> { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
-template <> struct WinVar<512, 2> { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+template <> struct WinVar<128, 1> : WinDef { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 4, 4>; };
+template <> struct WinVar<256, 1> : WinDef { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<256, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
+template <> struct WinVar<512, 1> : WinDef { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
+template <> struct WinVar<512, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
 // The faithful float window (PRC_FLAG_FAITHFUL_WINDOW) on variant 0's tiles
 // and plan: a launch code beside the variants, never chosen by the autotuner.
 constexpr int kWinFaithful = 7;
@@ -131,7 +139,9 @@ template <int N, int MODE> struct ColUsesWin {
 };
 template <int N, int MODE, int V> struct ColK {
   static constexpr int VV = MODE == TM_WIN ? V : 0;
-  using type = typename std::conditional<ColUsesWin<N, MODE>::v, CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P>,
+  using type = typename std::conditional<ColUsesWin<N, MODE>::v,
+                                         CK<N, WinVar<N, VV>::T, typename WinVar<N, VV>::P, WinVar<N, VV>::PPF,
+                                            WinVar<N, VV>::MINB>,
                                          CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
 };
 

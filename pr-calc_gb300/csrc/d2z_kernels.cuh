@@ -25,7 +25,7 @@
 
 namespace prc {
 
-constexpr int kMaxBatch = 32;  // radii per sweep at most
+constexpr int kMaxBatch = 64;  // radii per sweep at most
 constexpr int kNHistory = 100000;
 
 // ------------------------------------------------------------ per-N plans
