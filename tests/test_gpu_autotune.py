@@ -36,7 +36,7 @@ def test_every_variant_matches_default(N):
     with pytest.raises(prc_d2z.PrcError):
         ctx.tune(0, nv)
     with pytest.raises(prc_d2z.PrcError):
-        ctx.tune(33, 0)   # more radii per sweep than the kernels' parameter arrays hold
+        ctx.tune(65, 0)   # more radii per sweep than the kernels' parameter arrays hold
     ctx.close()
 
 
