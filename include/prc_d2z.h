@@ -260,17 +260,36 @@ int prc_d2z_last_timing(prc_d2z_ctx* ctx, float* ms3);
 int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
 
 /* ---- batches of boxes ------------------------------------------------------
- * Many independent boxes (realisations), possibly of different grid sizes:
- * one workspace per box, boxes spread over n_streams streams, and with
- * use_graph = 1 the kernels of all boxes captured once into a CUDA graph and
- * replayed with one launch per call (re-captured when the pointers change).
- * delta, zreion (and argmax, nullable) are arrays of n_boxes device pointers.
+ * Many independent boxes (realisations), possibly of different grid sizes,
+ * one workspace per box.  delta, zreion (and argmax, nullable) are arrays of
+ * n_boxes device pointers; every mode gives the same results bit for bit.
+ * Modes of prc_d2z_batch_forward:
+ *   PRC_BATCH_LOOP     each box's launches, boxes spread over n_streams streams;
+ *   PRC_BATCH_GRAPH    the same launches captured once into a CUDA graph and
+ *                      replayed with one launch per call (captured again when
+ *                      the pointers change);
+ *   PRC_BATCH_GROUPED  the boxes of each grid size form a group and every pass
+ *                      of the step runs as ONE launch over all boxes of the
+ *                      group: resident CTAs walk the (box, tile) or (box, line
+ *                      group) items of that pass, with each box's pointers,
+ *                      radius count and constants read from device tables;
+ *                      each group on its own stream, all captured once into a
+ *                      CUDA graph (about 3 + 3 x sweeps launches per grid size
+ *                      instead of as many per box).  The tables are rewritten
+ *                      at every call, so new pointers need no new capture.
+ *                      Grid sizes up to 256 except 8..24 and 48 have grouped
+ *                      kernels; boxes of other sizes run per box inside the same
+ *                      graph.  argmax: every box or none; the window pass uses
+ *                      variant 0 and the smallest radius batch of the group.
  * No reference counterpart: the reference processes one box per run. */
+#define PRC_BATCH_LOOP    0
+#define PRC_BATCH_GRAPH   1
+#define PRC_BATCH_GROUPED 2
 typedef struct prc_d2z_batch prc_d2z_batch;
 int prc_d2z_batch_create(int n_boxes, const prc_d2z_desc* descs, int n_streams, prc_d2z_batch** out);
 int prc_d2z_batch_tune(prc_d2z_batch* batch, int box, int radius_batch, int win_variant);
 int prc_d2z_batch_forward(prc_d2z_batch* batch, const float* const* delta, float* const* zreion,
-                          uint8_t* const* argmax, int use_graph);
+                          uint8_t* const* argmax, int mode);
 int prc_d2z_batch_launches(prc_d2z_batch* batch, int* n);
 int prc_d2z_batch_destroy(prc_d2z_batch* batch);
 

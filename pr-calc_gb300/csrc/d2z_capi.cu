@@ -483,6 +483,25 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, floa
 // Many boxes of (possibly) different sizes: one context per box, boxes spread
 // round-robin over a few streams, optionally all captured into one CUDA graph
 // and replayed with a single launch.
+// Grouped launches (PRC_BATCH_GROUPED): the boxes of one grid size form a
+// group, and every pass of the step runs as one launch over all boxes of the
+// group -- persistent CTAs (a grid of resident CTAs) walking the list of
+// (box, tile) or (box, line group) items of that pass -- instead of one launch
+// per box.  Each group has its own stream; the groups run side by side.  The
+// per-box pointers and constants sit in device tables, rewritten before each
+// forward (they carry the caller's input and output pointers), so the
+// captured graph of a grouped batch never needs capturing again.
+struct BatchGroup {
+  int N = 0, B = 0, nsweeps = 0;
+  std::vector<int> boxes;        // batch indices, largest radius count first
+  cudaStream_t st = nullptr;
+  // table offsets (bytes) in the batch's table buffer
+  size_t o_r2c = 0, o_fy = 0, o_fx = 0;
+  std::vector<size_t> o_win, o_inv, o_line;
+  std::vector<int> nsw;          // boxes taking part in sweep s (the first nsw[s] of `boxes`)
+  std::vector<int> nbmax;        // radii in sweep s of its largest box
+};
+
 struct prc_d2z_batch {
   int n = 0, dev = 0;
   std::vector<prc_d2z_ctx*> ctx;
@@ -492,6 +511,13 @@ struct prc_d2z_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<const void*> key;  // pointers the graph was captured with
+  int exec_mode = -1;            // batch mode the graph was captured in
+  // grouped launches
+  std::vector<BatchGroup> groups;
+  std::vector<cudaEvent_t> gev;  // one join event per group
+  std::vector<char> h_tab;       // host image of the tables
+  char* d_tab = nullptr;
+  int launches = 0;              // launches of the last grouped forward
 };
 
 namespace {
@@ -499,6 +525,10 @@ namespace {
 void batch_free(prc_d2z_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto& g : b->groups)
+    if (g.st) cudaStreamDestroy(g.st);
+  for (auto e : b->gev) cudaEventDestroy(e);
+  cudaFree(b->d_tab);
   for (auto* c : b->ctx) prc_d2z_destroy(c);
   for (auto e : b->ev) cudaEventDestroy(e);
   for (auto s : b->streams) cudaStreamDestroy(s);
@@ -518,6 +548,208 @@ void batch_enqueue(prc_d2z_batch* b, const float* const* delta, float* const* zr
     cudaEventRecord(b->ev[1 + k], b->streams[k]);
     cudaStreamWaitEvent(b->origin, b->ev[1 + k], 0);
   }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Groups of equal grid size, their sweeps and the layout of their tables.
+// Sizes without grouped kernels keep per-box launches (no group).
+int batch_group_setup(prc_d2z_batch* b) {
+  for (auto& g : b->groups)
+    if (g.st) cudaStreamDestroy(g.st);
+  for (auto e : b->gev) cudaEventDestroy(e);
+  b->groups.clear();
+  b->gev.clear();
+  cudaFree(b->d_tab);
+  b->d_tab = nullptr;
+  std::vector<int> sizes;
+  for (auto* c : b->ctx)
+    if (c->ksl.grouped && std::find(sizes.begin(), sizes.end(), c->N) == sizes.end()) sizes.push_back(c->N);
+  std::sort(sizes.begin(), sizes.end(), [](int x, int y) { return x > y; });
+  size_t off = 0;
+  for (int N : sizes) {
+    BatchGroup g;
+    g.N = N;
+    g.B = kMaxBatch;
+    int nrmax = 0;
+    for (int i = 0; i < b->n; ++i)
+      if (b->ctx[i]->N == N) {
+        g.boxes.push_back(i);
+        g.B = std::min(g.B, b->ctx[i]->B);
+        nrmax = std::max(nrmax, b->ctx[i]->nr);
+      }
+    // largest radius count first: the boxes of sweep s are then a prefix, in
+    // order of their radii in that sweep
+    std::stable_sort(g.boxes.begin(), g.boxes.end(), [&](int x, int y) { return b->ctx[x]->nr > b->ctx[y]->nr; });
+    g.nsweeps = (nrmax + g.B - 1) / g.B;
+    const size_t nb = g.boxes.size();
+    g.o_r2c = off;
+    off = align256(off + nb * sizeof(BoxR2c));
+    g.o_fy = off;
+    off = align256(off + nb * sizeof(BoxCol));
+    g.o_fx = off;
+    off = align256(off + nb * sizeof(BoxCol));
+    for (int sw = 0; sw < g.nsweeps; ++sw) {
+      int k = 0;
+      while (k < (int)nb && b->ctx[g.boxes[k]]->nr > sw * g.B) ++k;
+      g.nsw.push_back(k);
+      g.nbmax.push_back(std::min(g.B, b->ctx[g.boxes[0]]->nr - sw * g.B));
+      g.o_win.push_back(off);
+      off = align256(off + k * sizeof(BoxCol));
+      g.o_inv.push_back(off);
+      off = align256(off + k * sizeof(BoxCol));
+      g.o_line.push_back(off);
+      off = align256(off + k * sizeof(BoxLine));
+    }
+    b->groups.push_back(g);
+  }
+  b->h_tab.assign(off, 0);
+  if (off) {
+    int st;
+    if ((st = dalloc(&b->d_tab, off, "batch tables")) != PRC_OK) return st;
+  }
+  for (auto& g : b->groups) {
+    PRC_CU(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking), "group stream");
+    cudaEvent_t e;
+    PRC_CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "group event");
+    b->gev.push_back(e);
+  }
+  return PRC_OK;
+}
+
+// Host image of every group's tables for these inputs and outputs.
+void batch_group_fill(prc_d2z_batch* b, const float* const* delta, float* const* zreion, uint8_t* const* argmax) {
+  char* h = b->h_tab.data();
+  for (const auto& g : b->groups) {
+    for (size_t k = 0; k < g.boxes.size(); ++k) {
+      const int i = g.boxes[k];
+      const prc_d2z_ctx* c = b->ctx[i];
+      const long long NN = c->NN, H = c->H;
+      float2* S = c->spec;
+      BoxR2c r;
+      r.delta = delta[i];
+      r.S = S;
+      r.Qt = S + NN * (H + 1);
+      r.dinit = (float)c->dinit;
+      memcpy(h + g.o_r2c + k * sizeof(BoxR2c), &r, sizeof r);
+      BoxCol fy, fx;
+      memset(&fy, 0, sizeof fy);
+      memset(&fx, 0, sizeof fx);
+      // y pass: main in place, Nyquist Qt -> Q (transposed); x pass: both in place
+      fy.in0 = S, fy.out0 = S, fy.in1 = S + NN * (H + 1), fy.out1 = S + NN * H;
+      fx.in0 = S, fx.out0 = S, fx.in1 = S + NN * H, fx.out1 = S + NN * H;
+      memcpy(h + g.o_fy + k * sizeof(BoxCol), &fy, sizeof fy);
+      memcpy(h + g.o_fx + k * sizeof(BoxCol), &fx, sizeof fx);
+    }
+    for (int sw = 0; sw < g.nsweeps; ++sw) {
+      for (int k = 0; k < g.nsw[sw]; ++k) {
+        const int i = g.boxes[k];
+        const prc_d2z_ctx* c = b->ctx[i];
+        const long long NN = c->NN, H = c->H;
+        const int r0 = sw * g.B, nb = std::min(g.B, c->nr - r0);
+        float2* U = c->slots;
+        BoxCol w, v;
+        memset(&w, 0, sizeof w);
+        memset(&v, 0, sizeof v);
+        w.in0 = c->spec, w.out0 = U, w.in1 = c->spec + NN * H, w.out1 = U + NN * H, w.nb = nb;
+        for (int q = 0; q < nb; ++q) w.kr[q] = c->kr[r0 + q];
+        v.in0 = U, v.out0 = U, v.in1 = U + NN * H, v.out1 = U + NN * H, v.nb = nb;
+        memcpy(h + g.o_win[sw] + k * sizeof(BoxCol), &w, sizeof w);
+        memcpy(h + g.o_inv[sw] + k * sizeof(BoxCol), &v, sizeof v);
+        BoxLine L;
+        memset(&L, 0, sizeof L);
+        L.slots = U;
+        L.zreion = L.zreion_out = zreion[i];
+        L.argmax = L.argmax_out = argmax ? argmax[i] : nullptr;
+        L.nb = nb, L.r0 = r0, L.first = (sw == 0), L.as = c->as;
+        for (int q = 0; q < nb; ++q) L.cb[q] = c->cb[r0 + q];
+        memcpy(h + g.o_line[sw] + k * sizeof(BoxLine), &L, sizeof L);
+      }
+    }
+  }
+}
+
+// Every pass of every group as one launch over the group's boxes, groups on
+// their own streams; boxes of sizes without grouped kernels as per-box
+// launches on the batch's streams.  Kernels only (capturable).
+void batch_enqueue_grouped(prc_d2z_batch* b, const float* const* delta, float* const* zreion,
+                           uint8_t* const* argmax) {
+  cudaEventRecord(b->ev[0], b->origin);
+  for (auto& g : b->groups) cudaStreamWaitEvent(g.st, b->ev[0], 0);
+  for (auto s : b->streams) cudaStreamWaitEvent(s, b->ev[0], 0);
+  int launches = 0;
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    const BatchGroup& g = b->groups[gi];
+    const prc_d2z_ctx* c0 = b->ctx[g.boxes[0]];
+    const KernelSet& ks = c0->ksl;
+    const int N = g.N, H = N / 2, sms = c0->sms, nbox = (int)g.boxes.size();
+    const long long NN = c0->NN;
+    float2* S0 = c0->spec;
+    float2* U0 = c0->slots;
+    ks.r2c_z_mb(ks, grid_for(N * N * nbox, ks.line_groups, ks.occ_mb_r2c, sms), g.st,
+                reinterpret_cast<const BoxR2c*>(b->d_tab + g.o_r2c), nbox, c0->tw);
+    auto cols = [&](int mode, TileSeg s0, TileSeg s1, size_t o, int nboxes, int gy, const int* nvb) {
+      TileArgs a;
+      memset(&a, 0, sizeof(a));
+      if (mode == TM_WIN) {
+        s0.tpo = H / ks.tile_w_mb_win;
+        s1.tpo = N / ks.tile_w_mb_win;
+      }
+      a.seg[0] = s0;
+      a.seg[1] = s1;
+      a.slot_stride = c0->slot_f2;
+      a.tw = c0->tw;
+      a.box = reinterpret_cast<const BoxCol*>(b->d_tab + o);
+      a.nbox = nboxes;
+      if (nvb)
+        for (int y = 0; y < gy; ++y) a.nvb[y] = nvb[y];
+      const int tpb = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
+      const int occ = mode == TM_WIN ? ks.occ_mb_win : ks.occ_mb_tile;
+      ks.tile_mb(ks, mode, dim3(grid_for(tpb * (nvb ? nvb[0] : nboxes), 1, occ, sms), gy, 1), g.st, a);
+      ++launches;
+    };
+    cols(TM_FWD, mseg(c0, S0, S0, false), qseg(c0, S0 + NN * (H + 1), S0 + NN * H, true), g.o_fy, nbox, 1, nullptr);
+    cols(TM_FWD, mseg(c0, S0, S0, true), qseg(c0, S0 + NN * H, S0 + NN * H, false), g.o_fx, nbox, 1, nullptr);
+    for (int sw = 0; sw < g.nsweeps; ++sw) {
+      const int ns = g.nsw[sw];
+      cols(TM_WIN, mseg(c0, S0, U0, true), qseg(c0, S0 + NN * H, U0 + NN * H, true), g.o_win[sw], ns, 1, nullptr);
+      int nvb[kMaxBatch];
+      for (int y = 0; y < g.nbmax[sw]; ++y) {
+        int k = 0;
+        while (k < ns && b->ctx[g.boxes[k]]->nr - sw * g.B > y) ++k;
+        nvb[y] = k;
+      }
+      cols(TM_INV, mseg(c0, U0, U0, false), qseg(c0, U0 + NN * H, U0 + NN * H, false), g.o_inv[sw], ns,
+           g.nbmax[sw], nvb);
+      SweepArgs sa;
+      memset(&sa, 0, sizeof(sa));
+      sa.slot_stride = c0->slot_f2;
+      sa.tw = c0->tw;
+      sa.err = c0->err;
+      sa.argmax = argmax ? argmax[g.boxes[0]] : nullptr;
+      sa.box = reinterpret_cast<const BoxLine*>(b->d_tab + g.o_line[sw]);
+      sa.nbox = ns;
+      ks.c2r_z_mb(ks, grid_for(N * N * ns, ks.c2r_lines, ks.occ_mb_c2r, sms), g.st, sa);
+      launches += 2;
+    }
+    launches += 1;
+    cudaEventRecord(b->gev[gi], g.st);
+    cudaStreamWaitEvent(b->origin, b->gev[gi], 0);
+  }
+  // sizes without grouped kernels: per-box launches
+  for (int i = 0; i < b->n; ++i) {
+    prc_d2z_ctx* c = b->ctx[i];
+    if (c->ksl.grouped) continue;
+    c->launches = 0;
+    forward_r2c(c, delta[i], c->dinit);
+    enqueue_sweeps(c, zreion[i], argmax ? argmax[i] : nullptr, nullptr);
+    launches += c->launches;
+  }
+  for (size_t k = 0; k < b->streams.size(); ++k) {
+    cudaEventRecord(b->ev[1 + k], b->streams[k]);
+    cudaStreamWaitEvent(b->origin, b->ev[1 + k], 0);
+  }
+  b->launches = launches;
 }
 
 }  // namespace
@@ -1170,12 +1402,18 @@ int prc_d2z_batch_tune(prc_d2z_batch* b, int box, int radius_batch, int win_vari
   if (box < 0 || box >= b->n) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_tune: box %d outside 0..%d", box, b->n - 1);
   int st;
   if ((st = prc_d2z_tune(b->ctx[box], radius_batch, win_variant)) != PRC_OK) return st;
-  // the captured graph holds the old launches
+  // the captured graph holds the old launches, the groups the old radius batch
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   b->exec = nullptr;
   b->graph = nullptr;
   b->key.clear();
+  b->exec_mode = -1;
+  for (auto& g : b->groups)
+    if (g.st) cudaStreamDestroy(g.st);
+  for (auto e : b->gev) cudaEventDestroy(e);
+  b->groups.clear();
+  b->gev.clear();
   return PRC_OK;
 }
 
@@ -1224,14 +1462,67 @@ int prc_d2z_batch_create(int n_boxes, const prc_d2z_desc* descs, int n_streams, 
 }
 
 int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* const* zreion,
-                          uint8_t* const* argmax, int use_graph) {
+                          uint8_t* const* argmax, int mode) {
   if (!b || !delta || !zreion) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null argument");
+  if (mode < PRC_BATCH_LOOP || mode > PRC_BATCH_GROUPED)
+    return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: mode %d is not one of PRC_BATCH_*", mode);
   for (int i = 0; i < b->n; ++i)
     if (!delta[i] || !zreion[i]) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: null pointer for box %d", i);
+  if (mode == PRC_BATCH_GROUPED && argmax)
+    for (int i = 0; i < b->n; ++i)
+      if (!argmax[i])
+        return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_forward: grouped launches record every box's argmax or none "
+                                         "(box %d has none)", i);
   int cur = -1, st;
   PRC_CU(cudaGetDevice(&cur), "cudaGetDevice");
   if (cur != b->dev) PRC_CU(cudaSetDevice(b->dev), "cudaSetDevice");
-  if (!use_graph) {
+  if (mode == PRC_BATCH_GROUPED) {
+    // The grouped boxes' pointers live in the tables, so one capture serves
+    // every call with the same argmax choice; boxes of sizes without grouped
+    // kernels are captured with their pointers (recaptured when they change).
+    const int gkey = argmax ? 3 : 2;
+    if (b->groups.empty() && (st = batch_group_setup(b)) != PRC_OK) return st;
+    batch_group_fill(b, delta, zreion, argmax);
+    if (!b->h_tab.empty())
+      PRC_CU(cudaMemcpyAsync(b->d_tab, b->h_tab.data(), b->h_tab.size(), cudaMemcpyHostToDevice, b->origin),
+             "batch tables");
+    std::vector<const void*> key;
+    for (int i = 0; i < b->n; ++i)
+      if (!b->ctx[i]->ksl.grouped) {
+        key.push_back(delta[i]);
+        key.push_back(zreion[i]);
+        key.push_back(argmax ? argmax[i] : nullptr);
+      }
+    if (!b->exec || b->exec_mode != gkey || key != b->key) {
+      if (b->exec) cudaGraphExecDestroy(b->exec);
+      if (b->graph) cudaGraphDestroy(b->graph);
+      b->exec = nullptr;
+      b->graph = nullptr;
+      PRC_CU(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal), "begin capture");
+      batch_enqueue_grouped(b, delta, zreion, argmax);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(b->origin, &g);
+      if (e != cudaSuccess) return cuda_fail(e, "end capture");
+      b->graph = g;
+      PRC_CU(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+      b->exec_mode = gkey;
+      b->key = key;
+    }
+    PRC_CU(cudaGraphLaunch(b->exec, b->origin), "graph launch");
+    PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
+    for (auto* c : b->ctx)
+      if ((st = check_kernel_flag(c, "prc_d2z_batch_forward")) != PRC_OK) return st;
+    return PRC_OK;
+  }
+  if (b->exec_mode >= PRC_BATCH_GROUPED) {  // a grouped capture (2: without, 3: with argmax)
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->key.clear();
+  }
+  b->exec_mode = mode;
+  if (mode == PRC_BATCH_LOOP) {
     batch_enqueue(b, delta, zreion, argmax);
     PRC_CU(cudaGetLastError(), "prc_d2z_batch_forward");
     PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
@@ -1269,7 +1560,11 @@ int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* co
 int prc_d2z_batch_launches(prc_d2z_batch* b, int* n) {
   if (!b || !n) return prc_fail(PRC_ERR_INVALID, "prc_d2z_batch_launches: null argument");
   int t = 0;
-  for (auto* c : b->ctx) t += c->launches;
+  if (b->exec_mode >= PRC_BATCH_GROUPED) {
+    t = b->launches;
+  } else {
+    for (auto* c : b->ctx) t += c->launches;
+  }
   *n = t;
   return PRC_OK;
 }

@@ -145,7 +145,12 @@ template <int N, int MODE, int V> struct ColK {
                                          CK<N, CCfg<N>::T, typename CCfg<N>::P>>::type;
 };
 
-template <int N, int MODE, int V = 0>
+// MB (grouped launch): the tiles of a.nbox boxes of this grid size, box i's
+// segment pointers, radius count and dk * R_b from a.box[i]; tile ti is tile
+// ti mod (tiles of one box) of box ti / (tiles of one box).  The inverse y
+// pass takes slot blockIdx.y of the first a.nvb[blockIdx.y] boxes (those with
+// more than blockIdx.y slots: the boxes are sorted by nb, largest first).
+template <int N, int MODE, int V = 0, bool MB = false>
 __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE, V>::type::MINB) k_col(TileArgs a) {
   using KK = typename ColK<N, MODE, V>::type;
   using P = typename KK::P;
@@ -169,19 +174,31 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   }
   PPCol<T, G, FirstRadix<P>::v> buf{tws + KK::TW + c, KK::BUF};
   const CtaSync sync;
+  static_assert(!MB || MODE != TM_ACC, "no grouped adjoint pass");
   const long long yoff = (MODE == TM_FWD || MODE == TM_INV) ? (long long)blockIdx.y * a.slot_stride : 0;
   const int tiles0 = a.seg[0].n_outer * a.seg[0].tpo;
-  const int tiles = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;
+  const int tpb = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;  // tiles of one box
+  const int tiles = !MB ? tpb : tpb * (MODE == TM_INV ? a.nvb[blockIdx.y] : a.nbox);
 
   struct Where {
     TileSeg sg;
-    int outer, tc;
+    int outer, tc, bx;
     long long off;
   };
   auto where = [&](int ti) {
     Where w;
+    w.bx = 0;
+    if constexpr (MB) {
+      w.bx = ti / tpb;
+      ti -= w.bx * tpb;
+    }
     const bool sn = ti >= tiles0;
     w.sg = sn ? a.seg[1] : a.seg[0];
+    if constexpr (MB) {
+      const BoxCol* bc = a.box + w.bx;
+      w.sg.in = sn ? bc->in1 : bc->in0;
+      w.sg.out = sn ? bc->out1 : bc->out0;
+    }
     const int tl = sn ? ti - tiles0 : ti;
     w.outer = tl / w.sg.tpo;
     w.tc = tl - w.outer * w.sg.tpo;
@@ -296,11 +313,12 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       }
       auto radius = [&](int b, bool last) {
         float wv[E];
+        const float krb = MB ? __ldg(&a.box[w.bx].kr[b]) : s_kr[b];
         if constexpr (FW) {
 #pragma unroll
-          for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], s_kr[b]);
+          for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
         } else {
-          wvals(kq, s_kr[b], wv);
+          wvals(kq, krb, wv);
         }
         float2 v[E];
 #pragma unroll
@@ -317,8 +335,9 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
-      for (int b = 0; b < a.nb - 1; ++b) radius(b, false);
-      radius(a.nb - 1, true);
+      const int nbt = MB ? __ldg(&a.box[w.bx].nb) : a.nb;
+      for (int b = 0; b < nbt - 1; ++b) radius(b, false);
+      radius(nbt - 1, true);
     }
   } else {  // TM_ACC (output never transposed)
     for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {

@@ -11,6 +11,7 @@ constexpr int kMaxWinVariants = 3;  // window-pass variants per grid size (autot
 struct TileArgs;
 struct SweepArgs;
 struct AdjArgs;
+struct BoxR2c;
 
 struct KernelSet {
   int N;
@@ -33,6 +34,15 @@ struct KernelSet {
   void (*c2r_z)(const KernelSet&, int grid, cudaStream_t, const SweepArgs&);
   void (*adj_z)(const KernelSet&, int grid, cudaStream_t, const AdjArgs&);
   void (*c2r_plain)(const KernelSet&, int grid, cudaStream_t, const AdjArgs&);
+  // grouped launches (several boxes of this size per launch), when compiled
+  // for this size (grouped = 1): forward z pass, column passes (TM_FWD,
+  // TM_INV, TM_WIN with window variant 0), inverse z pass
+  int grouped;
+  int tile_w_mb_win;
+  int occ_mb_tile, occ_mb_win, occ_mb_c2r, occ_mb_r2c;
+  void (*r2c_z_mb)(const KernelSet&, int grid, cudaStream_t, const BoxR2c* box, int nbox, const float2* tw);
+  void (*tile_mb)(const KernelSet&, int mode, dim3 grid, cudaStream_t, const TileArgs&);
+  void (*c2r_z_mb)(const KernelSet&, int grid, cudaStream_t, const SweepArgs&);
 };
 
 // nullptr when N has no compiled plan

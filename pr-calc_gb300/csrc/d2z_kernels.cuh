@@ -107,8 +107,19 @@ struct TileSeg {
   int nyq;           // 1: the kz = H plane (window frequencies: fy = column, fz = H)
 };
 
+// One box of a grouped column pass (several boxes of one grid size in one
+// launch): its segment pointers, radii or slots of this sweep and dk * R_b.
+struct BoxCol {
+  const float2* in0;
+  float2* out0;
+  const float2* in1;
+  float2* out1;
+  int nb;
+  float kr[kMaxBatch];
+};
+
 struct TileArgs {
-  TileSeg seg[2];          // main array, Nyquist plane
+  TileSeg seg[2];          // main array, Nyquist plane (grouped: geometry only)
   long long slot_stride;   // plain: per blockIdx.y; WIN: per radius (out); ACC: per radius (in)
   const float2* tw;        // N-entry table e^{+2 pi i k/N}
   int nb, first;
@@ -116,6 +127,31 @@ struct TileArgs {
   int faithful;            // window pass: the reference's float window (kr holds R_b)
   float dk, kmax;          // faithful window: dk = 2 pi / box and kmax = dk * N, in float
   float kr[kMaxBatch];     // dk * R_b (faithful window: R_b)
+  // grouped launches: the boxes (sorted by nb, largest first), their count,
+  // and per slot y of the inverse y pass the number of boxes with nb > y
+  const BoxCol* box;
+  int nbox;
+  int nvb[kMaxBatch];
+};
+
+// One box of a grouped inverse z pass.
+struct BoxLine {
+  float2* slots;
+  float* zreion;
+  uint8_t* argmax;
+  float* zreion_out;
+  uint8_t* argmax_out;
+  int nb, r0, first;
+  float as;
+  float cb[kMaxBatch];
+};
+
+// One box of a grouped forward z pass.
+struct BoxR2c {
+  const float* delta;
+  float2* S;
+  float2* Qt;
+  float dinit;
 };
 
 struct SweepArgs {
@@ -135,6 +171,10 @@ struct SweepArgs {
   int first;            // first sweep: zreion/argmax not read
   float as;             // A / N^3
   float cb[kMaxBatch];  // A*B_b - 1 (NaN: never wins)
+  // grouped launches: the boxes, whose entries stand in for slots, zreion,
+  // argmax, zreion_out, argmax_out, nb, r0, first, as and cb above
+  const BoxLine* box;
+  int nbox;
 };
 
 enum TileMode { TM_FWD = 0, TM_INV = 1, TM_WIN = 2, TM_ACC = 3 };
@@ -667,9 +707,12 @@ __device__ __forceinline__ void line_c2r(float2 (&v)[LK<N>::E], float2 xh, float
 // ============================================================ forward z pass
 // Real line (N samples, divided by DInit) -> X[0..H-1] into S and X[H] into
 // the transposed Nyquist scratch Qt[iy][ix].
-template <int N>
+// MB (grouped launch): the lines of nbox boxes of this grid size, line l of
+// box l / N^2 with box i's input, spectrum and divisor from box[i].
+template <int N, bool MB = false>
 __global__ void __launch_bounds__(LK<N>::THREADS, LK<N>::MINB) k_r2c_z(const float* __restrict__ delta, float dinit,
-                                                             float2* S, float2* Qt, const float2* twg) {
+                                                             float2* S, float2* Qt, const float2* twg,
+                                                             const BoxR2c* box, int nbox) {
   using KK = LK<N>;
   constexpr int H = N / 2, E = KK::E, G = KK::G, NG = KK::NG;
   extern __shared__ float4 smem4[];
@@ -681,25 +724,39 @@ __global__ void __launch_bounds__(LK<N>::THREADS, LK<N>::MINB) k_r2c_z(const flo
   const int g = threadIdx.x / G, t = threadIdx.x % G;
   float2* gbuf = tws + KK::TW + g * KK::gsize;
   GroupSync<G> sync(g);
-  const int lines = N * N;
+  constexpr int lpb = N * N;  // lines of one box
+  static_assert(!MB || lpb % NG == 0, "a CTA step never spans two boxes");
+  const int lines = MB ? lpb * nbox : lpb;
   for (int s = blockIdx.x; s * NG < lines; s += gridDim.x) {
-    const int l = s * NG + g;
+    int l = s * NG + g;
     const bool valid = l < lines;
+    const float* dsrc = delta;
+    float dv = dinit;
+    float2 *Sb = S, *Qb = Qt;
+    if constexpr (MB) {
+      const int bx = (s * NG) / lpb;  // the same box for the whole step
+      const BoxR2c* bp = box + bx;
+      dsrc = bp->delta;
+      dv = bp->dinit;
+      Sb = bp->S;
+      Qb = bp->Qt;
+      l -= bx * lpb;
+    }
     float2 v[E];
-    const float2* src = reinterpret_cast<const float2*>(delta + (long long)(valid ? l : 0) * N);
+    const float2* src = reinterpret_cast<const float2*>(dsrc + (long long)(valid ? l : 0) * N);
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       float2 q = valid ? __ldg(src + t + G * m) : make_float2(0.f, 0.f);
-      v[m] = make_float2(__fdiv_rn(q.x, dinit), __fdiv_rn(q.y, dinit));
+      v[m] = make_float2(__fdiv_rn(q.x, dv), __fdiv_rn(q.y, dv));
     }
     const float xh = line_r2c<N>(v, gbuf, t, tw, tws, sync);
     if (valid) {
-      float2* dst = S + (long long)l * H;
+      float2* dst = Sb + (long long)l * H;
 #pragma unroll
       for (int m = 0; m < E; ++m) dst[t + G * m] = v[m];
       if (t == 0) {
         const int ix = l / N, iy = l - (l / N) * N;
-        Qt[(long long)iy * N + ix] = make_float2(xh, 0.f);
+        Qb[(long long)iy * N + ix] = make_float2(xh, 0.f);
       }
     }
   }

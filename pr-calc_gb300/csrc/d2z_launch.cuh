@@ -36,6 +36,7 @@ template <int N> struct ColLaunch<N, false> {
     }
     return 1;
   }
+  static constexpr bool GROUPED = false;
   static void launch(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     switch (mode) {
       case TM_FWD: k_tile<N, TM_FWD><<<grid, THREADS, TS, st>>>(a); break;
@@ -110,6 +111,20 @@ template <int N> struct ColLaunch<N, true> {
       default: k_col<N, TM_ACC><<<grid, CA::THREADS, CSA, st>>>(a); break;
     }
   }
+  // grouped launches (several boxes of this size per launch; window variant 0)
+  static constexpr bool GROUPED = N <= 256 && PCfg<N>::on;
+  using W0 = typename Win<0>::K;
+  static constexpr size_t WS0 = (size_t)W0::smem_f2 * sizeof(float2);
+  template <int MODE> static void* fn_mb() { return reinterpret_cast<void*>(&k_col<N, MODE, 0, true>); }
+  static void launch_mb(int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    if constexpr (GROUPED) {
+      switch (mode) {
+        case TM_FWD: k_col<N, TM_FWD, 0, true><<<grid, THREADS, CS, st>>>(a); break;
+        case TM_INV: k_col<N, TM_INV, 0, true><<<grid, THREADS, CS, st>>>(a); break;
+        default: k_col<N, TM_WIN, 0, true><<<grid, W0::THREADS, WS0, st>>>(a); break;
+      }
+    }
+  }
 };
 
 // Inverse z pass: k_c2r_zp (mirror pairs in one lane) where PCfg<N> has a
@@ -120,6 +135,7 @@ template <int N, bool PAIR = PCfg<N>::on> struct C2rLaunch {
   static constexpr int NFN = 1;
   static void* fn(int) { return reinterpret_cast<void*>(&k_c2r_z<N>); }
   static void launch(int grid, cudaStream_t st, const SweepArgs& a) { k_c2r_z<N><<<grid, THREADS, BYTES, st>>>(a); }
+  static void launch_mb(int, cudaStream_t, const SweepArgs&) {}
 };
 template <int N> struct C2rLaunch<N, true> {
   static constexpr int THREADS = PK<N>::THREADS, NG = PK<N>::NG;
@@ -135,6 +151,12 @@ template <int N> struct C2rLaunch<N, true> {
       if (a.argmax) k_c2r_zp<N, true, false><<<grid, THREADS, BYTES, st>>>(a);
       else k_c2r_zp<N, false, false><<<grid, THREADS, BYTES, st>>>(a);
     }
+  }
+  // grouped: a.argmax != null means every box of the launch records its argmax
+  template <bool AM> static void* f_mb() { return reinterpret_cast<void*>(&k_c2r_zp<N, AM, false, true>); }
+  static void launch_mb(int grid, cudaStream_t st, const SweepArgs& a) {
+    if (a.argmax) k_c2r_zp<N, true, false, true><<<grid, THREADS, BYTES, st>>>(a);
+    else k_c2r_zp<N, false, false, true><<<grid, THREADS, BYTES, st>>>(a);
   }
 };
 
@@ -173,6 +195,21 @@ template <int N> struct Launchers {
     }
     ks->occ_tile_win = ks->occ_winv[0];
     ks->tile_w_win = ks->tile_w_winv[0];
+    if constexpr (CL::GROUPED) {
+      void* fm = CL::template fn_mb<TM_FWD>();
+      void* im = CL::template fn_mb<TM_INV>();
+      void* wm = CL::template fn_mb<TM_WIN>();
+      if ((e = smem(fm, CL::CS)) != cudaSuccess) return e;
+      if ((e = smem(im, CL::CS)) != cudaSuccess) return e;
+      if ((e = smem(wm, CL::WS0)) != cudaSuccess) return e;
+      if ((e = smem(CR::template f_mb<false>(), CR::BYTES)) != cudaSuccess) return e;
+      if ((e = smem(CR::template f_mb<true>(), CR::BYTES)) != cudaSuccess) return e;
+      if ((e = smem(&k_r2c_z<N, true>, LS)) != cudaSuccess) return e;
+      if ((e = occ(&ks->occ_mb_tile, im, CL::THREADS, CL::CS)) != cudaSuccess) return e;
+      if ((e = occ(&ks->occ_mb_win, wm, CL::W0::THREADS, CL::WS0)) != cudaSuccess) return e;
+      if ((e = occ(&ks->occ_mb_c2r, CR::template f_mb<true>(), CR::THREADS, CR::BYTES)) != cudaSuccess) return e;
+      if ((e = occ(&ks->occ_mb_r2c, &k_r2c_z<N, true>, LL::THREADS, LS)) != cudaSuccess) return e;
+    }
     if ((e = smem(CL::faithful_fn(), CL::FS)) != cudaSuccess) return e;
     if ((e = occ(&ks->occ_win_faithful, CL::faithful_fn(), CL::FTHREADS, CL::FS)) != cudaSuccess) return e;
     if ((e = smem(&k_r2c_z<N>, LS)) != cudaSuccess) return e;
@@ -190,7 +227,16 @@ template <int N> struct Launchers {
   }
   static void r2c_z(const KernelSet&, int grid, cudaStream_t st, const float* d, float dinit, float2* S,
                     float2* Qt, const float2* tw) {
-    k_r2c_z<N><<<grid, LL::THREADS, LS, st>>>(d, dinit, S, Qt, tw);
+    k_r2c_z<N><<<grid, LL::THREADS, LS, st>>>(d, dinit, S, Qt, tw, nullptr, 0);
+  }
+  static void r2c_z_mb(const KernelSet&, int grid, cudaStream_t st, const BoxR2c* box, int nbox, const float2* tw) {
+    if constexpr (CL::GROUPED) k_r2c_z<N, true><<<grid, LL::THREADS, LS, st>>>(nullptr, 1.f, nullptr, nullptr, tw, box, nbox);
+  }
+  static void tile_mb(const KernelSet&, int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
+    CL::launch_mb(mode, grid, st, a);
+  }
+  static void c2r_z_mb(const KernelSet&, int grid, cudaStream_t st, const SweepArgs& a) {
+    if constexpr (CL::GROUPED) CR::launch_mb(grid, st, a);
   }
   static void tile(const KernelSet&, int mode, dim3 grid, cudaStream_t st, const TileArgs& a) {
     CL::launch(mode, grid, st, a);
@@ -220,6 +266,13 @@ template <int N> struct Launchers {
     ks.c2r_z = &c2r_z;
     ks.adj_z = &adj_z;
     ks.c2r_plain = &c2r_plain;
+    if constexpr (CL::GROUPED) {
+      ks.grouped = 1;
+      ks.tile_w_mb_win = CL::W0::T;
+      ks.r2c_z_mb = &r2c_z_mb;
+      ks.tile_mb = &tile_mb;
+      ks.c2r_z_mb = &c2r_z_mb;
+    }
     return ks;
   }
 };

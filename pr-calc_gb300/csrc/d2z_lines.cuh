@@ -112,8 +112,12 @@ constexpr int kWithheldPolls = 256;  // wait limit of a CTA whose copy the test 
 // first wait runs out for real, with nothing in flight.
 // AM: argmax wanted (a.argmax != null); its bytes are packed four to a register.
 // SIG: per-radius sums of x^2 wanted (a.sig_acc != null).
-template <int N, bool AM, bool SIG>
+// MB (grouped launch): the line groups of a.nbox boxes of this grid size, box
+// i's slots, outputs, radius count and barrier constants from a.box[i]; line
+// group q is line group q mod (N^2 / NG) of box q / (N^2 / NG).
+template <int N, bool AM, bool SIG, bool MB = false>
 __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArgs a) {
+  static_assert(!(MB && SIG), "no per-radius sums in grouped launches");
   using KK = PK<N>;
   using P = typename KK::P;
   constexpr int H = N / 2, E = KK::E, G = KK::G, NG = KK::NG, EH = E / 2, STG = KK::STG;
@@ -135,9 +139,14 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   const LineBuf<H> buf{gb + g * KK::gsize};
   GroupSync<G> sync(g);
   const int partner = (G - t) & (G - 1);
-  const int nsteps_l = (int)((NN / NG - blockIdx.x + gridDim.x - 1) / gridDim.x);  // line groups of this CTA
-  const int nb = a.nb;
-  const int total = nsteps_l > 0 ? nsteps_l * nb : 0;
+  constexpr long long lgpb = NN / NG;  // line groups of one box
+  const long long lg_all = MB ? lgpb * a.nbox : lgpb;
+  const int nsteps_l = (int)((lg_all - blockIdx.x + gridDim.x - 1) / gridDim.x);  // line groups of this CTA
+  // line group lg of this CTA: its box and its first line within that box
+  auto box_of = [&](int lg) { return MB ? (int)(((long long)blockIdx.x + (long long)lg * gridDim.x) / lgpb) : 0; };
+  auto line0 = [&](int lg, int bx) {
+    return ((long long)blockIdx.x + (long long)lg * gridDim.x - (long long)bx * lgpb) * NG;
+  };
 
   __shared__ __align__(8) uint64_t s_bar[2];
   if (threadIdx.x == 0) {
@@ -151,8 +160,9 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   const bool withheld = a.withhold && blockIdx.x == 0;
   auto issue = [&](int lg, int b, int bi) {
     if (lg < nsteps_l) {
-      const long long l0 = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG;
-      const float2* slot = a.slots + (long long)b * a.slot_stride;
+      const int bx = box_of(lg);
+      const long long l0 = line0(lg, bx);
+      const float2* slot = (MB ? a.box[bx].slots : a.slots) + (long long)b * a.slot_stride;
       if (threadIdx.x == 0 && !(withheld && lg == 0 && b == 0))
         bulk_load(stage + bi * STG, slot + l0 * H, STG * 8, &s_bar[bi]);
       if (t == 0) {
@@ -168,17 +178,20 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
   float2 zr[E];
   uint32_t am[AM ? EH : 1];  // argmax bytes of cells 2p, 2p+1 of elements 2j (low half) and 2j+1
   int lg = 0, b = 0;         // current step; steps run radius-fastest
-  for (int i = 0; i < total; ++i) {
+  for (int i = 0; lg < nsteps_l; ++i) {
     const int bi = i & 1;
+    const int bx = box_of(lg);
+    const BoxLine* bp = MB ? a.box + bx : nullptr;
+    const int nb = MB ? bp->nb : a.nb;
     const int nb_next = (b + 1 < nb) ? b + 1 : 0;
     const int lg_next = (b + 1 < nb) ? lg : lg + 1;
-    const long long l = ((long long)blockIdx.x + (long long)lg * gridDim.x) * NG + g;
-    float* zline = a.zreion + l * N;
-    uint16_t* aline = AM ? reinterpret_cast<uint16_t*>(a.argmax + l * N) : nullptr;
-    float* zout = a.zreion_out + l * N;
-    uint16_t* aout = AM ? reinterpret_cast<uint16_t*>(a.argmax_out + l * N) : nullptr;
+    const long long l = line0(lg, bx) + g;
+    float* zline = (MB ? bp->zreion : a.zreion) + l * N;
+    uint16_t* aline = AM ? reinterpret_cast<uint16_t*>((MB ? bp->argmax : a.argmax) + l * N) : nullptr;
+    float* zout = (MB ? bp->zreion_out : a.zreion_out) + l * N;
+    uint16_t* aout = AM ? reinterpret_cast<uint16_t*>((MB ? bp->argmax_out : a.argmax_out) + l * N) : nullptr;
     if (b == 0) {
-      if (a.first) {
+      if (MB ? bp->first : a.first) {
 #pragma unroll
         for (int m = 0; m < E; ++m) zr[m] = make_float2(0.f, 0.f);
         if constexpr (AM) {
@@ -244,13 +257,14 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
       v[EH] = make_float2(xe.x - xo.y, xe.y + xo.x);
     }
     PlanRun<P>::template run<true>(v, buf, t, tws, sync);
-    const float cb = s_cb[b];
-    const uint32_t rid = (uint32_t)(a.r0 + b);
+    const float cb = MB ? __ldg(&bp->cb[b]) : s_cb[b];
+    const float as = MB ? bp->as : a.as;
+    const uint32_t rid = (uint32_t)((MB ? bp->r0 : a.r0) + b);
     float ss = 0.f;
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       const float x0 = v[m].x, x1 = v[m].y;
-      const float z0 = fmaf(a.as, x0, cb), z1 = fmaf(a.as, x1, cb);
+      const float z0 = fmaf(as, x0, cb), z1 = fmaf(as, x1, cb);
       if constexpr (AM) {
         const int sh = 16 * (m & 1);
         if (z0 > zr[m].x) {

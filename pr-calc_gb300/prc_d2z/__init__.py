@@ -479,8 +479,10 @@ class Delta2Zreion:
 
 class Batch:
     """Many boxes (any mix of supported grid sizes) run together: one
-    workspace per box, n_streams CUDA streams, and with use_graph the kernels
-    of all boxes captured into one CUDA graph (prc_d2z_batch_*).
+    workspace per box, n_streams CUDA streams (prc_d2z_batch_*).  forward's
+    mode: "loop" (each box's launches), "graph" (those launches captured into
+    one CUDA graph) or "grouped" (one launch per pass over all boxes of a grid
+    size, the groups side by side, captured into one CUDA graph).
 
     boxes: list of dicts with the Delta2Zreion arguments (N, box_mpc,
     radii_mpc, barrier_b, barrier_a, growth_init, radius_batch)."""
@@ -508,8 +510,12 @@ class Batch:
         self._b = ctypes.c_void_p()
         check(L.prc_d2z_batch_create(self.n, descs, int(n_streams), ctypes.byref(self._b)))
 
-    def forward(self, deltas, zreions, argmaxes=None, use_graph: bool = True):
-        """deltas/zreions (/argmaxes): lists of contiguous CUDA tensors."""
+    MODES = {"loop": _lib.PRC_BATCH_LOOP, "graph": _lib.PRC_BATCH_GRAPH, "grouped": _lib.PRC_BATCH_GROUPED}
+
+    def forward(self, deltas, zreions, argmaxes=None, use_graph: bool = True, mode: str | None = None):
+        """deltas/zreions (/argmaxes): lists of contiguous CUDA tensors.  mode:
+        "loop", "graph" or "grouped" (default: "graph" if use_graph else "loop")."""
+        m = self.MODES[mode] if mode is not None else (_lib.PRC_BATCH_GRAPH if use_graph else _lib.PRC_BATCH_LOOP)
         L = load()
         n = self.n
         dp = (ctypes.c_void_p * n)(*[_dev_ptr(d.reshape(-1), "float32", self.N[i] ** 3).value
@@ -520,7 +526,7 @@ class Batch:
         if argmaxes is not None:
             ap = (ctypes.c_void_p * n)(*[_dev_ptr(a.reshape(-1), "uint8", self.N[i] ** 3).value
                                         for i, a in enumerate(argmaxes)])
-        check(L.prc_d2z_batch_forward(self._b, dp, zp, ap, 1 if use_graph else 0))
+        check(L.prc_d2z_batch_forward(self._b, dp, zp, ap, m))
         return zreions
 
     def launches(self) -> int:

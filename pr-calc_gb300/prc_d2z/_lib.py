@@ -20,6 +20,9 @@ PRC_ERR_NUMERIC = -6
 PRC_FLAG_ARGMAX = 1
 PRC_FLAG_SIGMA_GRID = 2
 PRC_FLAG_FAITHFUL_WINDOW = 4
+PRC_BATCH_LOOP = 0
+PRC_BATCH_GRAPH = 1
+PRC_BATCH_GROUPED = 2
 PRC_NHISTORY = 100000
 PRC_ARGMAX_NONE = 255
 PRC_MAX_RADII = 254
