@@ -460,17 +460,24 @@ def batched_measure(steps, warmup, streams):
     def run_batch(bt):
         bt.forward(deltas, outs_batch, mode="graph")
 
-    stream_ms = None
+    outs_grouped = [torch.empty_like(d) for d in deltas]
+
+    def run_grouped(bt):
+        bt.forward(deltas, outs_grouped, mode="grouped")
+
+    stream_ms = stream_ms_g = None
+    streams_g = streams
     if streams <= 0:
         streams, stream_ms = autotune.tune_batch_streams(make_batch, run_batch, streams=(1, 2, 4))
+        streams_g, stream_ms_g = autotune.tune_batch_streams(make_batch, run_grouped, streams=(1, 2, 3, 5))
     batch = make_batch(streams)
-    outs_grouped = [torch.empty_like(d) for d in deltas]
+    batch_g = make_batch(streams_g)
 
     def batched():
         run_batch(batch)
 
     def grouped():
-        batch.forward(deltas, outs_grouped, mode="grouped")
+        run_grouped(batch_g)
 
     res = {}
     for name, fn in (("loop", loop), ("batched", batched), ("grouped", grouped)):
@@ -488,7 +495,7 @@ def batched_measure(steps, warmup, streams):
     same = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_batch))
     same_g = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_grouped))
     ms_loop, ms_b, ms_g = res["loop"][0], res["batched"][0], res["grouped"][0]
-    launches_g = batch.launches()
+    launches_g = batch_g.launches()
     out = {"workload": "96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
                        "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
            "mode": "grouped: one launch per pass over all boxes of a grid size, sizes side by side, one graph",
@@ -497,9 +504,11 @@ def batched_measure(steps, warmup, streams):
            "per_box_graph": {"ms_per_step": ms_b, "value": work / (ms_b * 1e-3), "streams": streams,
                              "streams_ms": stream_ms, "identical_to_loop": bool(same), "clocks": res["batched"][1]},
            "speedup_vs_loop": ms_loop / ms_g, "identical_to_loop": bool(same_g),
+           "streams": streams_g, "streams_ms": stream_ms_g,
            "autotuned": {str(N): {"radius_batch": B, "win_variant": v} for N, (B, v) in tuning.items()},
            "gpu_launches": launches_g, "clocks": res["grouped"][1]}
     batch.close()
+    batch_g.close()
     for c in ctxs:
         c.close()
     del deltas, outs_loop, outs_batch, outs_grouped

@@ -273,8 +273,8 @@ int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
  *                      group: resident CTAs walk the (box, tile) or (box, line
  *                      group) items of that pass, with each box's pointers,
  *                      radius count and constants read from device tables;
- *                      each group on its own stream, all captured once into a
- *                      CUDA graph (about 3 + 3 x sweeps launches per grid size
+ *                      the groups share out the n_streams streams (largest
+ *                      grid size first), all captured once into a CUDA graph (about 3 + 3 x sweeps launches per grid size
  *                      instead of as many per box).  The tables are rewritten
  *                      at every call, so new pointers need no new capture.
  *                      Grid sizes up to 256 except 8..24 and 48 have grouped

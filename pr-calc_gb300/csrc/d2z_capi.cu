@@ -490,11 +490,12 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, floa
 // per box.  Each group has its own stream; the groups run side by side.  The
 // per-box pointers and constants sit in device tables, rewritten before each
 // forward (they carry the caller's input and output pointers), so the
-// captured graph of a grouped batch never needs capturing again.
+// captured graph of a grouped batch never needs capturing again.  The groups
+// share out the batch's n_streams streams, largest grid size first.
 struct BatchGroup {
   int N = 0, B = 0, nsweeps = 0;
   std::vector<int> boxes;        // batch indices, largest radius count first
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;    // one of the batch's streams (groups round-robin, largest first)
   // table offsets (bytes) in the batch's table buffer
   size_t o_r2c = 0, o_fy = 0, o_fx = 0;
   std::vector<size_t> o_win, o_inv, o_line;
@@ -525,8 +526,6 @@ namespace {
 void batch_free(prc_d2z_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  for (auto& g : b->groups)
-    if (g.st) cudaStreamDestroy(g.st);
   for (auto e : b->gev) cudaEventDestroy(e);
   cudaFree(b->d_tab);
   for (auto* c : b->ctx) prc_d2z_destroy(c);
@@ -555,8 +554,6 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Groups of equal grid size, their sweeps and the layout of their tables.
 // Sizes without grouped kernels keep per-box launches (no group).
 int batch_group_setup(prc_d2z_batch* b) {
-  for (auto& g : b->groups)
-    if (g.st) cudaStreamDestroy(g.st);
   for (auto e : b->gev) cudaEventDestroy(e);
   b->groups.clear();
   b->gev.clear();
@@ -608,8 +605,8 @@ int batch_group_setup(prc_d2z_batch* b) {
     int st;
     if ((st = dalloc(&b->d_tab, off, "batch tables")) != PRC_OK) return st;
   }
-  for (auto& g : b->groups) {
-    PRC_CU(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking), "group stream");
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    b->groups[gi].st = b->streams[gi % b->streams.size()];
     cudaEvent_t e;
     PRC_CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "group event");
     b->gev.push_back(e);
@@ -675,7 +672,6 @@ void batch_group_fill(prc_d2z_batch* b, const float* const* delta, float* const*
 void batch_enqueue_grouped(prc_d2z_batch* b, const float* const* delta, float* const* zreion,
                            uint8_t* const* argmax) {
   cudaEventRecord(b->ev[0], b->origin);
-  for (auto& g : b->groups) cudaStreamWaitEvent(g.st, b->ev[0], 0);
   for (auto s : b->streams) cudaStreamWaitEvent(s, b->ev[0], 0);
   int launches = 0;
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
@@ -1409,8 +1405,6 @@ int prc_d2z_batch_tune(prc_d2z_batch* b, int box, int radius_batch, int win_vari
   b->graph = nullptr;
   b->key.clear();
   b->exec_mode = -1;
-  for (auto& g : b->groups)
-    if (g.st) cudaStreamDestroy(g.st);
   for (auto e : b->gev) cudaEventDestroy(e);
   b->groups.clear();
   b->gev.clear();
