@@ -416,14 +416,18 @@ def _cfg_box(N, nr, seed, zeta, box=None, rmax=RMAX):
 
 def batched_measure(steps, warmup, streams):
     """96 realisations, grids 64/96/128/192/256 at 1.5 Mpc/h cells, 24-48 radii
-    each: per-box loop of the plain path vs one captured-graph batch launch.
-    Both use the autotuned radius batch and window-pass variant of each grid
-    size (prc_d2z.autotune); the batch also picks its stream count by timing.
-    Returns a dict (times, speed-up, bit-identity, clocks)."""
+    each: a per-box loop of the plain path, the same launches captured in one
+    graph, and grouped launches (one launch per pass and grid size).  Every box
+    sweeps all its radii at once (radius batch = its radius count: one read of
+    its spectrum and one write of its zreion, the fastest batch at every size)
+    with the autotuned window-pass variant of its grid size; each batch mode
+    picks its stream count by timing.  The modes run one after another, each
+    freeing its workspaces before the next.  Returns a dict (times, speed-ups,
+    bit-identity, clocks)."""
     import torch
 
     import prc_d2z
-    from prc_d2z import fields
+    from prc_d2z import autotune, fields
     rng = np.random.default_rng(2024)
     sizes = [64] * 20 + [96] * 19 + [128] * 19 + [192] * 19 + [256] * 19
     rng.shuffle(sizes)
@@ -431,87 +435,79 @@ def batched_measure(steps, warmup, streams):
     boxes, deltas = [], []
     for i, (N, nr) in enumerate(zip(sizes, nrs)):
         b, box = _cfg_box(int(N), int(nr), 1000 + i, ZETA_BATCH)
+        b["radius_batch"] = int(nr)
         boxes.append(b)
         deltas.append(fields.gaussian_field(int(N), box, seed=1000 + i, backend="torch").contiguous())
     work = sum(b["N"] ** 3 * len(b["radii_mpc"]) for b in boxes)
-    outs_loop = [torch.empty_like(d) for d in deltas]
-    outs_batch = [torch.empty_like(d) for d in deltas]
-    # autotuned radius batch and window-pass variant per grid size (cached)
-    from prc_d2z import autotune
     nr_rep = int(np.median(nrs))
-    tuning = {int(N): autotune.tuned(int(N), nr_rep) for N in sorted(set(sizes))}
-    for b in boxes:
-        b["radius_batch"] = tuning[b["N"]][0]
-    ctxs = [prc_d2z.Delta2Zreion(b["N"], b["box_mpc"], b["radii_mpc"], b["barrier_b"], b["barrier_a"],
-                                 b["growth_init"], radius_batch=b["radius_batch"], argmax=False) for b in boxes]
-    for c, b in zip(ctxs, boxes):
-        c.tune(0, tuning[b["N"]][1])
+    variant = {int(N): autotune.tuned(int(N), nr_rep)[1] for N in sorted(set(sizes))}
 
-    def loop():
-        for c, d, o in zip(ctxs, deltas, outs_loop):
-            c.forward(d, zreion=o, want_argmax=False)
-
-    def make_batch(n_streams):
-        bt = prc_d2z.Batch(boxes, n_streams=n_streams)
-        for i, b in enumerate(boxes):
-            bt.tune(i, 0, tuning[b["N"]][1])
-        return bt
-
-    def run_batch(bt):
-        bt.forward(deltas, outs_batch, mode="graph")
-
-    outs_grouped = [torch.empty_like(d) for d in deltas]
-
-    def run_grouped(bt):
-        bt.forward(deltas, outs_grouped, mode="grouped")
-
-    stream_ms = stream_ms_g = None
-    streams_g = streams
-    if streams <= 0:
-        streams, stream_ms = autotune.tune_batch_streams(make_batch, run_batch, streams=(1, 2, 4))
-        streams_g, stream_ms_g = autotune.tune_batch_streams(make_batch, run_grouped, streams=(1, 2, 3, 5))
-    batch = make_batch(streams)
-    batch_g = make_batch(streams_g)
-
-    def batched():
-        run_batch(batch)
-
-    def grouped():
-        run_grouped(batch_g)
-
-    res = {}
-    for name, fn in (("loop", loop), ("batched", batched), ("grouped", grouped)):
+    def timed(fn):
         for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with Clocks(0) as clk:
+        with Clocks(torch.cuda.current_device()) as clk:
             e0.record()
             for _ in range(steps):
                 fn()
             e1.record()
             torch.cuda.synchronize()
-        res[name] = (e0.elapsed_time(e1) / steps, clk.summary())
-    same = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_batch))
-    same_g = all(torch.equal(a, b) for a, b in zip(outs_loop, outs_grouped))
-    ms_loop, ms_b, ms_g = res["loop"][0], res["batched"][0], res["grouped"][0]
-    launches_g = batch_g.launches()
+        return e0.elapsed_time(e1) / steps, clk.summary()
+
+    # the plain per-box loop
+    outs_loop = [torch.empty_like(d) for d in deltas]
+    ctxs = [prc_d2z.Delta2Zreion(b["N"], b["box_mpc"], b["radii_mpc"], b["barrier_b"], b["barrier_a"],
+                                 b["growth_init"], radius_batch=b["radius_batch"], argmax=False) for b in boxes]
+    for c, b in zip(ctxs, boxes):
+        c.tune(0, variant[b["N"]])
+
+    def loop():
+        for c, d, o in zip(ctxs, deltas, outs_loop):
+            c.forward(d, zreion=o, want_argmax=False)
+
+    ms_loop, clk_loop = timed(loop)
+    for c in ctxs:
+        c.close()
+    del ctxs
+    torch.cuda.empty_cache()
+
+    def make_batch(n_streams):
+        bt = prc_d2z.Batch(boxes, n_streams=n_streams)
+        for i, b in enumerate(boxes):
+            bt.tune(i, 0, variant[b["N"]])
+        return bt
+
+    res = {}
+    for mode, choices in (("graph", (1, 2, 4)), ("grouped", (1, 2, 3, 5))):
+        outs = [torch.empty_like(d) for d in deltas]
+
+        def run(bt, mode=mode, outs=outs):
+            bt.forward(deltas, outs, mode=mode)
+
+        ns, ns_ms = streams, None
+        if streams <= 0:
+            ns, ns_ms = autotune.tune_batch_streams(make_batch, run, streams=choices)
+        bt = make_batch(ns)
+        ms, clk = timed(lambda: run(bt))
+        res[mode] = {"ms_per_step": ms, "value": work / (ms * 1e-3), "streams": ns, "streams_ms": ns_ms,
+                     "identical_to_loop": all(torch.equal(a, o) for a, o in zip(outs_loop, outs)),
+                     "gpu_launches": bt.launches(), "clocks": clk}
+        bt.close()
+        del outs
+        torch.cuda.empty_cache()
+    g = res["grouped"]
     out = {"workload": "96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
                        "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
            "mode": "grouped: one launch per pass over all boxes of a grid size, sizes side by side, one graph",
-           "steps": steps, "warmup": warmup, "ms_per_step": ms_g, "value": work / (ms_g * 1e-3), "unit": UNIT,
-           "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3), "clocks": res["loop"][1]},
-           "per_box_graph": {"ms_per_step": ms_b, "value": work / (ms_b * 1e-3), "streams": streams,
-                             "streams_ms": stream_ms, "identical_to_loop": bool(same), "clocks": res["batched"][1]},
-           "speedup_vs_loop": ms_loop / ms_g, "identical_to_loop": bool(same_g),
-           "streams": streams_g, "streams_ms": stream_ms_g,
-           "autotuned": {str(N): {"radius_batch": B, "win_variant": v} for N, (B, v) in tuning.items()},
-           "gpu_launches": launches_g, "clocks": res["grouped"][1]}
-    batch.close()
-    batch_g.close()
-    for c in ctxs:
-        c.close()
-    del deltas, outs_loop, outs_batch, outs_grouped
+           "radius_batch": "each box's radius count (one sweep per box)",
+           "steps": steps, "warmup": warmup, "ms_per_step": g["ms_per_step"], "value": g["value"], "unit": UNIT,
+           "per_box_loop": {"ms_per_step": ms_loop, "value": work / (ms_loop * 1e-3), "clocks": clk_loop},
+           "per_box_graph": res["graph"], "grouped": g,
+           "speedup_vs_loop": ms_loop / g["ms_per_step"], "identical_to_loop": g["identical_to_loop"],
+           "win_variant": {str(N): v for N, v in variant.items()},
+           "gpu_launches": g["gpu_launches"], "clocks": g["clocks"]}
+    del deltas, outs_loop
     torch.cuda.empty_cache()
     return out
 
@@ -524,9 +520,10 @@ def run_batched(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (Philox4x32-10 + BBKS, seeds 1000..1095)",
         "config": {"workload": "batched: " + r["workload"], "zeta": ZETA_BATCH},
-        "mode": r["mode"], "per_box_loop": r["per_box_loop"], "per_box_graph": r["per_box_graph"],
-        "speedup_vs_loop": r["speedup_vs_loop"], "identical_to_loop": r["identical_to_loop"],
-        "autotuned": r["autotuned"], "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}), flush=True)
+        "mode": r["mode"], "radius_batch": r["radius_batch"], "per_box_loop": r["per_box_loop"],
+        "per_box_graph": r["per_box_graph"], "speedup_vs_loop": r["speedup_vs_loop"],
+        "identical_to_loop": r["identical_to_loop"], "win_variant": r["win_variant"],
+        "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}), flush=True)
 
 
 def adjoint_measure(N, steps, warmup, batch=0):

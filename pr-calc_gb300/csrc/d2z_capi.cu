@@ -493,14 +493,15 @@ void enqueue_sweeps(prc_d2z_ctx* c, float* d_z, uint8_t* d_am, double* sig, floa
 // captured graph of a grouped batch never needs capturing again.  The groups
 // share out the batch's n_streams streams, largest grid size first.
 struct BatchGroup {
-  int N = 0, B = 0, nsweeps = 0;
-  std::vector<int> boxes;        // batch indices, largest radius count first
+  int N = 0, nsweeps = 0;
+  std::vector<int> boxes;        // batch indices
   cudaStream_t st = nullptr;    // one of the batch's streams (groups round-robin, largest first)
   // table offsets (bytes) in the batch's table buffer
   size_t o_r2c = 0, o_fy = 0, o_fx = 0;
   std::vector<size_t> o_win, o_inv, o_line;
-  std::vector<int> nsw;          // boxes taking part in sweep s (the first nsw[s] of `boxes`)
-  std::vector<int> nbmax;        // radii in sweep s of its largest box
+  // sweep s: the boxes that have one (each box sweeps its own radius batch),
+  // most radii in that sweep first, and their radii in it
+  std::vector<std::vector<int>> sw_box, sw_nb;
 };
 
 struct prc_d2z_batch {
@@ -567,18 +568,25 @@ int batch_group_setup(prc_d2z_batch* b) {
   for (int N : sizes) {
     BatchGroup g;
     g.N = N;
-    g.B = kMaxBatch;
-    int nrmax = 0;
     for (int i = 0; i < b->n; ++i)
       if (b->ctx[i]->N == N) {
         g.boxes.push_back(i);
-        g.B = std::min(g.B, b->ctx[i]->B);
-        nrmax = std::max(nrmax, b->ctx[i]->nr);
+        const prc_d2z_ctx* c = b->ctx[i];
+        g.nsweeps = std::max(g.nsweeps, (c->nr + c->B - 1) / c->B);
       }
-    // largest radius count first: the boxes of sweep s are then a prefix, in
-    // order of their radii in that sweep
-    std::stable_sort(g.boxes.begin(), g.boxes.end(), [&](int x, int y) { return b->ctx[x]->nr > b->ctx[y]->nr; });
-    g.nsweeps = (nrmax + g.B - 1) / g.B;
+    for (int sw = 0; sw < g.nsweeps; ++sw) {
+      std::vector<int> bx;
+      for (int i : g.boxes)
+        if (b->ctx[i]->nr > sw * b->ctx[i]->B) bx.push_back(i);
+      auto nb_of = [&](int i) { return std::min(b->ctx[i]->B, b->ctx[i]->nr - sw * b->ctx[i]->B); };
+      // most radii first: the boxes with more than y radii in the sweep are a
+      // prefix, which the inverse y pass's slot y takes
+      std::stable_sort(bx.begin(), bx.end(), [&](int x, int y) { return nb_of(x) > nb_of(y); });
+      std::vector<int> nbs;
+      for (int i : bx) nbs.push_back(nb_of(i));
+      g.sw_box.push_back(bx);
+      g.sw_nb.push_back(nbs);
+    }
     const size_t nb = g.boxes.size();
     g.o_r2c = off;
     off = align256(off + nb * sizeof(BoxR2c));
@@ -587,10 +595,7 @@ int batch_group_setup(prc_d2z_batch* b) {
     g.o_fx = off;
     off = align256(off + nb * sizeof(BoxCol));
     for (int sw = 0; sw < g.nsweeps; ++sw) {
-      int k = 0;
-      while (k < (int)nb && b->ctx[g.boxes[k]]->nr > sw * g.B) ++k;
-      g.nsw.push_back(k);
-      g.nbmax.push_back(std::min(g.B, b->ctx[g.boxes[0]]->nr - sw * g.B));
+      const size_t k = g.sw_box[sw].size();
       g.o_win.push_back(off);
       off = align256(off + k * sizeof(BoxCol));
       g.o_inv.push_back(off);
@@ -639,11 +644,11 @@ void batch_group_fill(prc_d2z_batch* b, const float* const* delta, float* const*
       memcpy(h + g.o_fx + k * sizeof(BoxCol), &fx, sizeof fx);
     }
     for (int sw = 0; sw < g.nsweeps; ++sw) {
-      for (int k = 0; k < g.nsw[sw]; ++k) {
-        const int i = g.boxes[k];
+      for (size_t k = 0; k < g.sw_box[sw].size(); ++k) {
+        const int i = g.sw_box[sw][k];
         const prc_d2z_ctx* c = b->ctx[i];
         const long long NN = c->NN, H = c->H;
-        const int r0 = sw * g.B, nb = std::min(g.B, c->nr - r0);
+        const int r0 = sw * c->B, nb = g.sw_nb[sw][k];
         float2* U = c->slots;
         BoxCol w, v;
         memset(&w, 0, sizeof w);
@@ -707,22 +712,23 @@ void batch_enqueue_grouped(prc_d2z_batch* b, const float* const* delta, float* c
     cols(TM_FWD, mseg(c0, S0, S0, false), qseg(c0, S0 + NN * (H + 1), S0 + NN * H, true), g.o_fy, nbox, 1, nullptr);
     cols(TM_FWD, mseg(c0, S0, S0, true), qseg(c0, S0 + NN * H, S0 + NN * H, false), g.o_fx, nbox, 1, nullptr);
     for (int sw = 0; sw < g.nsweeps; ++sw) {
-      const int ns = g.nsw[sw];
+      const int ns = (int)g.sw_box[sw].size();
+      const std::vector<int>& nbs = g.sw_nb[sw];
       cols(TM_WIN, mseg(c0, S0, U0, true), qseg(c0, S0 + NN * H, U0 + NN * H, true), g.o_win[sw], ns, 1, nullptr);
       int nvb[kMaxBatch];
-      for (int y = 0; y < g.nbmax[sw]; ++y) {
+      for (int y = 0; y < nbs[0]; ++y) {
         int k = 0;
-        while (k < ns && b->ctx[g.boxes[k]]->nr - sw * g.B > y) ++k;
+        while (k < ns && nbs[k] > y) ++k;
         nvb[y] = k;
       }
-      cols(TM_INV, mseg(c0, U0, U0, false), qseg(c0, U0 + NN * H, U0 + NN * H, false), g.o_inv[sw], ns,
-           g.nbmax[sw], nvb);
+      cols(TM_INV, mseg(c0, U0, U0, false), qseg(c0, U0 + NN * H, U0 + NN * H, false), g.o_inv[sw], ns, nbs[0],
+           nvb);
       SweepArgs sa;
       memset(&sa, 0, sizeof(sa));
       sa.slot_stride = c0->slot_f2;
       sa.tw = c0->tw;
       sa.err = c0->err;
-      sa.argmax = argmax ? argmax[g.boxes[0]] : nullptr;
+      sa.argmax = argmax ? argmax[g.sw_box[sw][0]] : nullptr;
       sa.box = reinterpret_cast<const BoxLine*>(b->d_tab + g.o_line[sw]);
       sa.nbox = ns;
       ks.c2r_z_mb(ks, grid_for(N * N * ns, ks.c2r_lines, ks.occ_mb_c2r, sms), g.st, sa);

@@ -53,11 +53,11 @@ def test_batch_matches_per_box(mode):
 
 
 def test_grouped_batch_argmax_new_pointers_and_radius_batches():
-    """Grouped launches with argmax, with sweeps of unequal length per box
-    (radius batch 4: 3 to 17 radii make 1 to 5 sweeps), and with new output
+    """Grouped launches with argmax, with each box's own radius batch (4, 16
+    or 3: 1 to 6 sweeps of unequal length per box), and with new output
     buffers on the second call (the tables change, the capture stays)."""
     import torch
-    boxes, fields_ = zip(*[_box(N, nr, 200 + i, radius_batch=4) for i, (N, nr) in enumerate(SPEC)])
+    boxes, fields_ = zip(*[_box(N, nr, 200 + i, radius_batch=(4, 16, 3)[i % 3]) for i, (N, nr) in enumerate(SPEC)])
     ref = _reference(boxes, fields_, True)
     batch = prc_d2z.Batch(list(boxes), n_streams=2)
     dev = [torch.from_numpy(d).cuda() for d in fields_]
@@ -69,8 +69,8 @@ def test_grouped_batch_argmax_new_pointers_and_radius_batches():
         for (rz, ra), o, a in zip(ref, out, am):
             assert np.array_equal(o.cpu().numpy(), rz)
             assert np.array_equal(a.cpu().numpy(), ra)
-    # 2 groups (32: 5 sweeps, 64: 3 sweeps, 96: 2 sweeps => 3 + 3 x sweeps each)
-    # plus the per-box launches of the other sizes
+    # the groups of 32, 64 and 96 (3 + 3 x sweeps launches each) plus the
+    # per-box launches of the other sizes
     assert batch.launches() < sum(1 for _ in SPEC) * 10
     batch.close()
 
