@@ -77,7 +77,7 @@ def _time_forward(ctx, delta, z, reps: int) -> float:
     return statistics.median(ts)
 
 
-def tune(N: int, n_radii: int, reps: int = 3, force: bool = False, path: str | None = None) -> dict:
+def tune(N: int, n_radii: int, reps: int = 5, force: bool = False, path: str | None = None) -> dict:
     """Measure (or read from the cache) the fastest radius batch and window
     variant for N and n_radii; returns the cache entry."""
     import torch
@@ -93,13 +93,17 @@ def tune(N: int, n_radii: int, reps: int = 3, force: bool = False, path: str | N
     batches, variants = candidates(N, n_radii)
     delta = fields.gaussian_field(N, box, seed=1, backend="native")
     z = torch.empty_like(delta)
-    times = {}
+    # rounds over all candidates (not one candidate after another), so that a
+    # slow drift of the clocks under sustained load biases none of them
+    samples = {}
     with Delta2Zreion(N, float(np.float32(box) / np.float32(p.h)), t.radii_mpc, t.barrier_b, t.barrier_a, t.DInit,
                       radius_batch=max(batches), argmax=False) as ctx:
-        for B in batches:
-            for v in variants:
-                ctx.tune(B, v)
-                times[f"B{B}_v{v}"] = _time_forward(ctx, delta, z, reps)
+        for _ in range(reps):
+            for B in batches:
+                for v in variants:
+                    ctx.tune(B, v)
+                    samples.setdefault(f"B{B}_v{v}", []).append(_time_forward(ctx, delta, z, 1))
+    times = {k: statistics.median(v) for k, v in samples.items()}
     best = min(times, key=times.get)
     B, v = (int(x[1:]) for x in best.split("_"))
     entry = {"radius_batch": B, "win_variant": v, "ms": times[best], "times_ms": times}
