@@ -112,8 +112,11 @@ struct CtaSync {
 // one or two exchange buffers, measured 9.3-9.8 ms per 32-radius launch
 // against 5.05 ms for the register-held tile: at 80 registers the transform
 // spills, and the re-reads wait in its critical path.)
-constexpr int kWinVariants = 3;
-struct WinDef { static constexpr int PPF = -1, MINB = 0; };
+constexpr int kWinVariants = 4;
+// TABLE: W(|k| R_b) is read from a table over the integer |m|^2 (filled per
+// sweep by k_wtab with the same arithmetic, so the values are identical)
+// instead of evaluated per element.
+struct WinDef { static constexpr int PPF = -1, MINB = 0; static constexpr bool TABLE = false; };
 template <int N, int V> struct WinVar : WinDef { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
 template <int N> struct WinVar<N, 0> : WinDef {
   static constexpr bool on = CCfg<N>::on;
@@ -125,6 +128,14 @@ template <> struct WinVar<256, 1> : WinDef { static constexpr bool on = true; st
 template <> struct WinVar<256, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
 template <> struct WinVar<512, 1> : WinDef { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
 template <> struct WinVar<512, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
+template <> struct WinVar<256, 3> : WinDef {
+  static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16>;
+  static constexpr bool TABLE = true;
+};
+template <> struct WinVar<512, 3> : WinDef {
+  static constexpr bool on = true; static constexpr int T = 8; using P = Plan<16, 16, 16, 2>;
+  static constexpr bool TABLE = true;
+};
 // The faithful float window (PRC_FLAG_FAITHFUL_WINDOW) on variant 0's tiles
 // and plan: a launch code beside the variants, never chosen by the autotuner.
 constexpr int kWinFaithful = 7;
@@ -180,14 +191,17 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   const int tpb = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;  // tiles of one box
   const int tiles = !MB ? tpb : tpb * (MODE == TM_INV ? a.nvb[blockIdx.y] : a.nbox);
 
-  struct Where {
+  struct WhereS {
     TileSeg sg;
-    int outer, tc, bx;
+    int outer, tc;
     long long off;
   };
+  struct WhereM : WhereS {
+    int bx;  // the tile's box (grouped launches)
+  };
+  using Where = typename std::conditional<MB, WhereM, WhereS>::type;
   auto where = [&](int ti) {
     Where w;
-    w.bx = 0;
     if constexpr (MB) {
       w.bx = ti / tpb;
       ti -= w.bx * tpb;
@@ -233,9 +247,23 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       kq[m] = (m2 == 0) ? -1.f : sqrtf((float)m2);
     }
   };
-  // W(|k| R_b) of all E rows: rows m > E/2 mirror rows of the partner lane
-  // (lane ^ 16, FFT lane G - t, register E-1-m) or of this lane (t = 0: E-m;
-  // t = G/2: E-1-m)
+  // |m|^2 of the same rows (table windows)
+  auto kint = [&](const Where& w, int (&km)[EH + 1]) {
+    const int col = w.tc * T + c;
+    const int syz = w.sg.nyq ? fsq(col, N) + H * H : fsq(w.outer, N) + col * col;
+#pragma unroll
+    for (int m = 0; m <= EH; ++m) km[m] = fsq(t + G * m, N) + syz;
+  };
+  // rows m > E/2 mirror rows of the partner lane (lane ^ 16, FFT lane G - t,
+  // register E-1-m) or of this lane (t = 0: E-m; t = G/2: E-1-m)
+  auto mirror = [&](float (&wv)[E]) {
+#pragma unroll
+    for (int m = EH + 1; m < E; ++m) {
+      const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
+      wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
+    }
+  };
+  // W(|k| R_b) of all E rows
   // (the Taylor branch runs only in warps where some lane needs it)
   auto wvals = [&](const float (&kq)[EH + 1], float kr, float (&wv)[E]) {
     bool small = false;
@@ -255,11 +283,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
 #pragma unroll
     for (int m = 0; m <= EH; ++m)
       if (kq[m] < 0.f) wv[m] = 0.f;
-#pragma unroll
-    for (int m = EH + 1; m < E; ++m) {
-      const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
-      wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
-    }
+    mirror(wv);
   };
 
   if constexpr ((MODE == TM_FWD || MODE == TM_INV) && E <= 16 && KK::THREADS <= 512) {
@@ -292,8 +316,10 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       gstore(w, w.sg.out + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
-    // FW: the reference's float window, every row evaluated on its own
+    // FW: the reference's float window, every row evaluated on its own;
+    // TB: the window read from the per-sweep table over |m|^2
     constexpr bool FW = (V == kWinFaithful);
+    constexpr bool TB = WinVar<N, V>::TABLE;
     float2 raw[E];
     int ti = blockIdx.x;
     if (ti < tiles) {
@@ -302,23 +328,35 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     }
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
-      float kq[FW ? E : EH + 1];
+      float kq[TB ? 1 : (FW ? E : EH + 1)];
+      int km[TB ? EH + 1 : 1];
       if constexpr (FW) {
         const int col = w.tc * T + c;
         const int iy = w.sg.nyq ? col : w.outer, iz = w.sg.nyq ? H : col;
 #pragma unroll
         for (int m = 0; m < E; ++m) kq[m] = rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax);
+      } else if constexpr (TB) {
+        kint(w, km);
       } else {
         kmag(w, kq);
       }
       auto radius = [&](int b, bool last) {
         float wv[E];
-        const float krb = MB ? __ldg(&a.box[w.bx].kr[b]) : s_kr[b];
-        if constexpr (FW) {
+        if constexpr (TB) {
+          const float* tb = a.wtab + (long long)b * a.wtab_stride;
 #pragma unroll
-          for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
+          for (int m = 0; m <= EH; ++m) wv[m] = __ldg(tb + km[m]);
+          mirror(wv);
         } else {
-          wvals(kq, krb, wv);
+          float krb;
+          if constexpr (MB) krb = __ldg(&a.box[w.bx].kr[b]);
+          else krb = s_kr[b];
+          if constexpr (FW) {
+#pragma unroll
+            for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
+          } else {
+            wvals(kq, krb, wv);
+          }
         }
         float2 v[E];
 #pragma unroll
@@ -335,7 +373,9 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
-      const int nbt = MB ? __ldg(&a.box[w.bx].nb) : a.nb;
+      int nbt;
+      if constexpr (MB) nbt = __ldg(&a.box[w.bx].nb);
+      else nbt = a.nb;
       for (int b = 0; b < nbt - 1; ++b) radius(b, false);
       radius(nbt - 1, true);
     }
