@@ -218,8 +218,6 @@ struct prc_d2z_ctx {
   float* gstage = nullptr;
   uint8_t* amstage = nullptr;
   float* grf_amp = nullptr;       // field generator: amplitude by |m|^2
-  float* wtab = nullptr;          // table windows: W(|m| dk R_b) of a sweep's radii by |m|^2
-  int wtab_b = 0;                 // radii the table holds
   int* err = nullptr;             // set by a kernel whose copy wait ran out
   // prc_d2z_forward_many: two device copies of a box's input and outputs and
   // two copy streams (in, out), so that the copies of neighbouring boxes run
@@ -320,7 +318,6 @@ void free_all(prc_d2z_ctx* c) {
   cudaFree(c->gstage);
   cudaFree(c->amstage);
   cudaFree(c->grf_amp);
-  cudaFree(c->wtab);
   cudaFree(c->err);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -365,27 +362,12 @@ TileSeg qseg(const prc_d2z_ctx* c, const float2* in, float2* out, bool transpose
   return s;
 }
 
-// W(sqrt(q) * kr_b) for q = 0 .. stride-1 of the radii of one sweep (0 at
-// q = 0), with the arithmetic of the window pass's own evaluation, so that a
-// table variant multiplies by the very same values.
-__global__ void k_wtab(float* wt, int stride, int nb, TileArgs a) {
-  __shared__ float s_kr[kMaxBatch];
-  stage_params(s_kr, a.kr);
-  __syncthreads();
-  const long long n = (long long)nb * stride;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(i / stride), q = (int)(i - (long long)b * stride);
-    wt[i] = window_of(q, s_kr[b]);
-  }
-}
-
 // one column pass over the main array and the Nyquist plane
 void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb = 1, int r0 = 0, int first = 0) {
   TileArgs a;
   memset(&a, 0, sizeof(a));
   const bool faithful = mode == TM_WIN && (c->flags & PRC_FLAG_FAITHFUL_WINDOW);
-  int wv = faithful ? 0 : c->win_var;  // the faithful window runs on variant 0's tiles
-  if (mode == TM_WIN && c->ksl.win_table[wv] && (!c->wtab || c->wtab_b < nb)) wv = 0;  // no table: variant 0
+  const int wv = faithful ? 0 : c->win_var;  // the faithful window runs on variant 0's tiles
   if (mode == TM_WIN || mode == TM_ACC) {  // these passes may use narrower tiles
     const int tw = mode == TM_WIN ? c->ksl.tile_w_winv[wv] : c->ksl.tile_w_acc;
     s0.tpo = (s0.nyq ? c->N : c->H) / tw;
@@ -407,16 +389,6 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
     for (int b = 0; b < nb; ++b) a.kr[b] = (float)c->R[r0 + b];
   } else if (mode == TM_WIN || mode == TM_ACC) {
     for (int b = 0; b < nb; ++b) a.kr[b] = c->kr[r0 + b];
-  }
-  if (mode == TM_WIN && c->ksl.win_table[wv]) {
-    // the sweep's window table over |m|^2 (stride 3 (N/2)^2 + 1), allocated
-    // by prc_d2z_tune when it chose this variant
-    const int stride = 3 * c->H * c->H + 1;
-    k_wtab<<<grid_for((int)std::min<long long>((long long)nb * stride, 1LL << 30), 256, 4, c->sms), 256, 0, c->st>>>(
-        c->wtab, stride, nb, a);
-    c->launches++;
-    a.wtab = c->wtab;
-    a.wtab_stride = stride;
   }
   const int tiles = s0.n_outer * s0.tpo + s1.n_outer * s1.tpo;
   const int occ = (mode == TM_ACC) ? c->ksl.occ_tile_acc
@@ -1421,15 +1393,6 @@ int prc_d2z_tune(prc_d2z_ctx* c, int radius_batch, int win_variant) {
     cudaFree(c->slots);
     c->slots = ns;
     c->slots_b = B;
-  }
-  if (c->ksl.win_table[win_variant] && c->wtab_b < B) {  // a window table for B radii
-    if ((st = set_device(c)) != PRC_OK) return st;
-    PRC_CU(cudaStreamSynchronize(c->st), "prc_d2z_tune");
-    float* nt = nullptr;
-    if ((st = dalloc(&nt, (size_t)(3 * c->H * c->H + 1) * B, "window table")) != PRC_OK) return st;
-    cudaFree(c->wtab);
-    c->wtab = nt;
-    c->wtab_b = B;
   }
   c->B = B;
   c->win_var = win_variant;

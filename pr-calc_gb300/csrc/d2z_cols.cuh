@@ -112,11 +112,12 @@ struct CtaSync {
 // one or two exchange buffers, measured 9.3-9.8 ms per 32-radius launch
 // against 5.05 ms for the register-held tile: at 80 registers the transform
 // spills, and the re-reads wait in its critical path.)
-constexpr int kWinVariants = 4;
-// TABLE: W(|k| R_b) is read from a table over the integer |m|^2 (filled per
-// sweep by k_wtab with the same arithmetic, so the values are identical)
-// instead of evaluated per element.
-struct WinDef { static constexpr int PPF = -1, MINB = 0; static constexpr bool TABLE = false; };
+constexpr int kWinVariants = 3;
+// (A variant that reads W(|k| R_b) from a per-sweep table over the integer
+// |m|^2, filled with the same arithmetic so the results were bit-identical,
+// was measured at N = 256 and 512 and left out: the table reads are gathers
+// that miss L1, 8.9 against 5.2 ms per 32-radius launch at 512.)
+struct WinDef { static constexpr int PPF = -1, MINB = 0; };
 template <int N, int V> struct WinVar : WinDef { static constexpr bool on = false; static constexpr int T = 16; using P = void; };
 template <int N> struct WinVar<N, 0> : WinDef {
   static constexpr bool on = CCfg<N>::on;
@@ -128,14 +129,6 @@ template <> struct WinVar<256, 1> : WinDef { static constexpr bool on = true; st
 template <> struct WinVar<256, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 4>; };
 template <> struct WinVar<512, 1> : WinDef { static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16, 2>; };
 template <> struct WinVar<512, 2> : WinDef { static constexpr bool on = true; static constexpr int T = 8; using P = Plan<8, 8, 8, 8>; };
-template <> struct WinVar<256, 3> : WinDef {
-  static constexpr bool on = true; static constexpr int T = 16; using P = Plan<16, 16, 16>;
-  static constexpr bool TABLE = true;
-};
-template <> struct WinVar<512, 3> : WinDef {
-  static constexpr bool on = true; static constexpr int T = 8; using P = Plan<16, 16, 16, 2>;
-  static constexpr bool TABLE = true;
-};
 // The faithful float window (PRC_FLAG_FAITHFUL_WINDOW) on variant 0's tiles
 // and plan: a launch code beside the variants, never chosen by the autotuner.
 constexpr int kWinFaithful = 7;
@@ -191,9 +184,12 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   const int tpb = tiles0 + a.seg[1].n_outer * a.seg[1].tpo;  // tiles of one box
   const int tiles = !MB ? tpb : tpb * (MODE == TM_INV ? a.nvb[blockIdx.y] : a.nbox);
 
+  // A tile: its segment (0 main, 1 Nyquist plane), outer index, column
+  // block and offset; the segment's fields are read from the kernel
+  // parameters when used (selected, never indexed, so they stay in the
+  // parameter bank) rather than held in registers across the radii.
   struct WhereS {
-    TileSeg sg;
-    int outer, tc;
+    int sn, outer, tc;
     long long off;
   };
   struct WhereM : WhereS {
@@ -206,19 +202,32 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       w.bx = ti / tpb;
       ti -= w.bx * tpb;
     }
-    const bool sn = ti >= tiles0;
-    w.sg = sn ? a.seg[1] : a.seg[0];
-    if constexpr (MB) {
-      const BoxCol* bc = a.box + w.bx;
-      w.sg.in = sn ? bc->in1 : bc->in0;
-      w.sg.out = sn ? bc->out1 : bc->out0;
-    }
-    const int tl = sn ? ti - tiles0 : ti;
-    w.outer = tl / w.sg.tpo;
-    w.tc = tl - w.outer * w.sg.tpo;
-    w.off = (long long)w.outer * w.sg.outer_stride + (long long)w.tc * T;
+    w.sn = ti >= tiles0;
+    const int tl = w.sn ? ti - tiles0 : ti;
+    const int tpo = w.sn ? a.seg[1].tpo : a.seg[0].tpo;
+    w.outer = tl / tpo;
+    w.tc = tl - w.outer * tpo;
+    w.off = (long long)w.outer * (w.sn ? a.seg[1].outer_stride : a.seg[0].outer_stride) + (long long)w.tc * T;
     return w;
   };
+  auto sg_in = [&](const Where& w) -> const float2* {
+    if constexpr (MB) {
+      const BoxCol* bc = a.box + w.bx;
+      return w.sn ? bc->in1 : bc->in0;
+    } else {
+      return w.sn ? a.seg[1].in : a.seg[0].in;
+    }
+  };
+  auto sg_out = [&](const Where& w) -> float2* {
+    if constexpr (MB) {
+      const BoxCol* bc = a.box + w.bx;
+      return w.sn ? bc->out1 : bc->out0;
+    } else {
+      return w.sn ? a.seg[1].out : a.seg[0].out;
+    }
+  };
+  auto sg_rs = [&](const Where& w) { return w.sn ? a.seg[1].row_stride : a.seg[0].row_stride; };
+  auto sg_nyq = [&](const Where& w) { return w.sn ? a.seg[1].nyq : a.seg[0].nyq; };
   auto gload = [&](const float2* base, int rs, float2 (&v)[E]) {
     const float2* p = base + (long long)t * rs + c;
     const long long step = (long long)G * rs;
@@ -226,13 +235,15 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     for (int m = 0; m < E; ++m) v[m] = __ldg(p + m * step);
   };
   auto gstore = [&](const Where& w, float2* dst, const float2 (&v)[E]) {
-    if (w.sg.transpose) {
-      float2* q = dst + (long long)w.outer * w.sg.outer_stride + (long long)(w.tc * T + c) * N + t;
+    if (w.sn ? a.seg[1].transpose : a.seg[0].transpose) {
+      float2* q = dst + (long long)w.outer * (w.sn ? a.seg[1].outer_stride : a.seg[0].outer_stride) +
+                  (long long)(w.tc * T + c) * N + t;
 #pragma unroll
       for (int m = 0; m < E; ++m) q[G * m] = v[m];
     } else {
-      float2* q = dst + w.off + (long long)t * w.sg.row_stride + c;
-      const long long step = (long long)G * w.sg.row_stride;
+      const int rs = sg_rs(w);
+      float2* q = dst + w.off + (long long)t * rs + c;
+      const long long step = (long long)G * rs;
 #pragma unroll
       for (int m = 0; m < E; ++m) q[m * step] = v[m];
     }
@@ -240,19 +251,12 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   // |k| of rows t + G*m, m <= E/2, of this thread's column (-1: k = 0)
   auto kmag = [&](const Where& w, float (&kq)[EH + 1]) {
     const int col = w.tc * T + c;
-    const int syz = w.sg.nyq ? fsq(col, N) + H * H : fsq(w.outer, N) + col * col;
+    const int syz = sg_nyq(w) ? fsq(col, N) + H * H : fsq(w.outer, N) + col * col;
 #pragma unroll
     for (int m = 0; m <= EH; ++m) {
       const int m2 = fsq(t + G * m, N) + syz;
       kq[m] = (m2 == 0) ? -1.f : sqrtf((float)m2);
     }
-  };
-  // |m|^2 of the same rows (table windows)
-  auto kint = [&](const Where& w, int (&km)[EH + 1]) {
-    const int col = w.tc * T + c;
-    const int syz = w.sg.nyq ? fsq(col, N) + H * H : fsq(w.outer, N) + col * col;
-#pragma unroll
-    for (int m = 0; m <= EH; ++m) km[m] = fsq(t + G * m, N) + syz;
   };
   // rows m > E/2 mirror rows of the partner lane (lane ^ 16, FFT lane G - t,
   // register E-1-m) or of this lane (t = 0: E-m; t = G/2: E-1-m)
@@ -291,17 +295,17 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     int ti = blockIdx.x;
     if (ti < tiles) {
       const Where w = where(ti);
-      gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
+      gload(sg_in(w) + w.off + yoff, sg_rs(w), v);
     }
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
       const int tn = ti + gridDim.x;
       if (tn < tiles) {
         const Where wn = where(tn);
-        gload(wn.sg.in + wn.off + yoff, wn.sg.row_stride, nx);
+        gload(sg_in(wn) + wn.off + yoff, sg_rs(wn), nx);
       }
       PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
-      gstore(w, w.sg.out + yoff, v);
+      gstore(w, sg_out(w) + yoff, v);
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = nx[m];
     }
@@ -311,52 +315,40 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
       float2 v[E];
-      gload(w.sg.in + w.off + yoff, w.sg.row_stride, v);
+      gload(sg_in(w) + w.off + yoff, sg_rs(w), v);
       PlanRun<P>::template run<INV, KK::PP>(v, buf, t, tws, sync);
-      gstore(w, w.sg.out + yoff, v);
+      gstore(w, sg_out(w) + yoff, v);
     }
   } else if constexpr (MODE == TM_WIN) {
-    // FW: the reference's float window, every row evaluated on its own;
-    // TB: the window read from the per-sweep table over |m|^2
+    // FW: the reference's float window, every row evaluated on its own
     constexpr bool FW = (V == kWinFaithful);
-    constexpr bool TB = WinVar<N, V>::TABLE;
     float2 raw[E];
     int ti = blockIdx.x;
     if (ti < tiles) {
       const Where w = where(ti);
-      gload(w.sg.in + w.off, w.sg.row_stride, raw);
+      gload(sg_in(w) + w.off, sg_rs(w), raw);
     }
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
-      float kq[TB ? 1 : (FW ? E : EH + 1)];
-      int km[TB ? EH + 1 : 1];
+      float kq[FW ? E : EH + 1];
       if constexpr (FW) {
         const int col = w.tc * T + c;
-        const int iy = w.sg.nyq ? col : w.outer, iz = w.sg.nyq ? H : col;
+        const int iy = sg_nyq(w) ? col : w.outer, iz = sg_nyq(w) ? H : col;
 #pragma unroll
         for (int m = 0; m < E; ++m) kq[m] = rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax);
-      } else if constexpr (TB) {
-        kint(w, km);
       } else {
         kmag(w, kq);
       }
       auto radius = [&](int b, bool last) {
         float wv[E];
-        if constexpr (TB) {
-          const float* tb = a.wtab + (long long)b * a.wtab_stride;
+        float krb;
+        if constexpr (MB) krb = __ldg(&a.box[w.bx].kr[b]);
+        else krb = s_kr[b];
+        if constexpr (FW) {
 #pragma unroll
-          for (int m = 0; m <= EH; ++m) wv[m] = __ldg(tb + km[m]);
-          mirror(wv);
+          for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
         } else {
-          float krb;
-          if constexpr (MB) krb = __ldg(&a.box[w.bx].kr[b]);
-          else krb = s_kr[b];
-          if constexpr (FW) {
-#pragma unroll
-            for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
-          } else {
-            wvals(kq, krb, wv);
-          }
+          wvals(kq, krb, wv);
         }
         float2 v[E];
 #pragma unroll
@@ -366,11 +358,11 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
           const int tn = ti + gridDim.x;
           if (tn < tiles) {
             const Where wn = where(tn);
-            gload(wn.sg.in + wn.off, wn.sg.row_stride, raw);
+            gload(sg_in(wn) + wn.off, sg_rs(wn), raw);
           }
         }
         PlanRun<P>::template run<true, KK::PP>(v, buf, t, tws, sync);
-        gstore(w, w.sg.out + (long long)b * a.slot_stride, v);
+        gstore(w, sg_out(w) + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
       int nbt;
@@ -389,7 +381,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
       for (int b = 0; b < a.nb; ++b) {
         float2 v[E];
-        gload(w.sg.in + w.off + (long long)b * a.slot_stride, w.sg.row_stride, v);
+        gload(sg_in(w) + w.off + (long long)b * a.slot_stride, sg_rs(w), v);
         PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
         float wv[E];
         wvals(kq, s_kr[b], wv);
@@ -399,8 +391,9 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
           acc[m].y = fmaf(wv[m], v[m].y, acc[m].y);
         }
       }
-      float2* q = w.sg.out + w.off + (long long)t * w.sg.row_stride + c;
-      const long long step = (long long)G * w.sg.row_stride;
+      const int rs = sg_rs(w);
+      float2* q = sg_out(w) + w.off + (long long)t * rs + c;
+      const long long step = (long long)G * rs;
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         float2 o = a.first ? make_float2(0.f, 0.f) : q[m * step];

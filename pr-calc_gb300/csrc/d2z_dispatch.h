@@ -6,7 +6,7 @@
 
 namespace prc {
 
-constexpr int kMaxWinVariants = 4;  // window-pass variants per grid size (autotuned)
+constexpr int kMaxWinVariants = 3;  // window-pass variants per grid size (autotuned)
 
 struct TileArgs;
 struct SweepArgs;
@@ -19,7 +19,6 @@ struct KernelSet {
   int tile_w_win;               // columns per tile of the window pass (variant 0)
   int n_win_var;                // window-pass variants compiled for this N
   int tile_w_winv[kMaxWinVariants], occ_winv[kMaxWinVariants];  // per variant
-  int win_table[kMaxWinVariants];  // 1: the variant reads the per-sweep window table
   int tile_w_acc;               // columns per tile of the accumulate pass (adjoint)
   int line_threads, line_groups;  // threads per line-pass CTA, lines per CTA step
   int c2r_lines;                  // lines per CTA step of the inverse z pass

@@ -126,8 +126,6 @@ struct TileArgs {
   int win_var;             // window-pass variant (host-side launch choice)
   int faithful;            // window pass: the reference's float window (kr holds R_b)
   float dk, kmax;          // faithful window: dk = 2 pi / box and kmax = dk * N, in float
-  const float* wtab;       // table windows: W of radius b at |m|^2 = q is wtab[b * wtab_stride + q]
-  int wtab_stride;
   float kr[kMaxBatch];     // dk * R_b (faithful window: R_b)
   // grouped launches: the boxes (sorted by nb, largest first), their count,
   // and per slot y of the inverse y pass the number of boxes with nb > y

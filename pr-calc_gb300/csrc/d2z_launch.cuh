@@ -27,14 +27,12 @@ template <int N> struct ColLaunch<N, false> {
   static int threads(int) { return THREADS; }
   static constexpr int T_ACC = T;
   // one window variant: the staged tile kernel
-  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr,
-                 int* tab = nullptr) {
+  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr) {
     if (v == 0) {
       if (f) *f = reinterpret_cast<void*>(&k_tile<N, TM_WIN>);
       if (thr) *thr = THREADS;
       if (by) *by = TS2;
       if (tw) *tw = T;
-      if (tab) *tab = 0;
     }
     return 1;
   }
@@ -64,7 +62,7 @@ template <int N> struct ColLaunch<N, true> {
   template <int MODE> static void* fn() { return reinterpret_cast<void*>(&k_col<N, MODE>); }
   static size_t bytes(int mode) { return mode == TM_ACC ? CSA : CS; }
   static int threads(int mode) { return mode == TM_ACC ? CA::THREADS : THREADS; }
-  template <int V> static void win_info(int v, int* n, void** f, int* thr, size_t* by, int* tw, int* tab) {
+  template <int V> static void win_info(int v, int* n, void** f, int* thr, size_t* by, int* tw) {
     if constexpr (V < kWinVariants) {
       if constexpr (Win<V>::on) {
         if (v == V) {
@@ -72,21 +70,18 @@ template <int N> struct ColLaunch<N, true> {
           *thr = Win<V>::K::THREADS;
           *by = (size_t)Win<V>::K::smem_f2 * sizeof(float2);
           *tw = Win<V>::K::T;
-          *tab = WinVar<N, V>::TABLE ? 1 : 0;
         }
         *n = V + 1;
       }
-      win_info<V + 1>(v, n, f, thr, by, tw, tab);
+      win_info<V + 1>(v, n, f, thr, by, tw);
     }
   }
-  // number of window variants and, for variant v, its kernel, threads, bytes,
-  // tile width and whether it reads a window table
-  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr,
-                 int* tab = nullptr) {
-    int n = 0, t0 = 0, w0 = 0, x0 = 0;
+  // number of window variants and, for variant v, its kernel, threads, bytes, tile width
+  static int win(int v, void** f = nullptr, int* thr = nullptr, size_t* by = nullptr, int* tw = nullptr) {
+    int n = 0, t0 = 0, w0 = 0;
     void* f0 = nullptr;
     size_t b0 = 0;
-    win_info<0>(v, &n, f ? f : &f0, thr ? thr : &t0, by ? by : &b0, tw ? tw : &w0, tab ? tab : &x0);
+    win_info<0>(v, &n, f ? f : &f0, thr ? thr : &t0, by ? by : &b0, tw ? tw : &w0);
     return n;
   }
   using WF = typename ColK<N, TM_WIN, kWinFaithful>::type;
@@ -191,13 +186,12 @@ template <int N> struct Launchers {
     ks->n_win_var = CL::win(0);
     for (int v = 0; v < ks->n_win_var; ++v) {
       void* f = nullptr;
-      int thr = 0, tw = 0, tab = 0;
+      int thr = 0, tw = 0;
       size_t by = 0;
-      CL::win(v, &f, &thr, &by, &tw, &tab);
+      CL::win(v, &f, &thr, &by, &tw);
       if ((e = smem(f, by)) != cudaSuccess) return e;
       if ((e = occ(&ks->occ_winv[v], f, thr, by)) != cudaSuccess) return e;
       ks->tile_w_winv[v] = tw;
-      ks->win_table[v] = tab;
     }
     ks->occ_tile_win = ks->occ_winv[0];
     ks->tile_w_win = ks->tile_w_winv[0];
