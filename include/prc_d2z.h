@@ -280,7 +280,8 @@ int prc_d2z_last_launches(prc_d2z_ctx* ctx, int* n);
  *                      Grid sizes up to 256 except 8..24 and 48 have grouped
  *                      kernels; boxes of other sizes run per box inside the same
  *                      graph.  argmax: every box or none; each box keeps its
- *                      own radius batch; the window pass uses variant 0.
+ *                      own radius batch; the window pass uses variant 0 (boxes
+ *                      with PRC_FLAG_FAITHFUL_WINDOW run per box).
  * No reference counterpart: the reference processes one box per run. */
 #define PRC_BATCH_LOOP    0
 #define PRC_BATCH_GRAPH   1

@@ -552,6 +552,10 @@ void batch_enqueue(prc_d2z_batch* b, const float* const* delta, float* const* zr
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// A box joins a grouped launch when its size has grouped kernels and it asks
+// for nothing they leave out (the faithful window runs per box).
+bool groupable(const prc_d2z_ctx* c) { return c->ksl.grouped && !(c->flags & PRC_FLAG_FAITHFUL_WINDOW); }
+
 // Groups of equal grid size, their sweeps and the layout of their tables.
 // Sizes without grouped kernels keep per-box launches (no group).
 int batch_group_setup(prc_d2z_batch* b) {
@@ -562,14 +566,14 @@ int batch_group_setup(prc_d2z_batch* b) {
   b->d_tab = nullptr;
   std::vector<int> sizes;
   for (auto* c : b->ctx)
-    if (c->ksl.grouped && std::find(sizes.begin(), sizes.end(), c->N) == sizes.end()) sizes.push_back(c->N);
+    if (groupable(c) && std::find(sizes.begin(), sizes.end(), c->N) == sizes.end()) sizes.push_back(c->N);
   std::sort(sizes.begin(), sizes.end(), [](int x, int y) { return x > y; });
   size_t off = 0;
   for (int N : sizes) {
     BatchGroup g;
     g.N = N;
     for (int i = 0; i < b->n; ++i)
-      if (b->ctx[i]->N == N) {
+      if (b->ctx[i]->N == N && groupable(b->ctx[i])) {
         g.boxes.push_back(i);
         const prc_d2z_ctx* c = b->ctx[i];
         g.nsweeps = std::max(g.nsweeps, (c->nr + c->B - 1) / c->B);
@@ -741,7 +745,7 @@ void batch_enqueue_grouped(prc_d2z_batch* b, const float* const* delta, float* c
   // sizes without grouped kernels: per-box launches
   for (int i = 0; i < b->n; ++i) {
     prc_d2z_ctx* c = b->ctx[i];
-    if (c->ksl.grouped) continue;
+    if (groupable(c)) continue;
     c->launches = 0;
     forward_r2c(c, delta[i], c->dinit);
     enqueue_sweeps(c, zreion[i], argmax ? argmax[i] : nullptr, nullptr);
@@ -1488,7 +1492,7 @@ int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* co
              "batch tables");
     std::vector<const void*> key;
     for (int i = 0; i < b->n; ++i)
-      if (!b->ctx[i]->ksl.grouped) {
+      if (!groupable(b->ctx[i])) {
         key.push_back(delta[i]);
         key.push_back(zreion[i]);
         key.push_back(argmax ? argmax[i] : nullptr);

@@ -485,7 +485,8 @@ class Batch:
     size, the groups side by side, captured into one CUDA graph).
 
     boxes: list of dicts with the Delta2Zreion arguments (N, box_mpc,
-    radii_mpc, barrier_b, barrier_a, growth_init, radius_batch)."""
+    radii_mpc, barrier_b, barrier_a, growth_init, radius_batch,
+    faithful_window)."""
 
     def __init__(self, boxes, n_streams: int = 4):
         L = load()
@@ -506,7 +507,7 @@ class Batch:
             d.barrier_a = float(b["barrier_a"])
             d.growth_init = float(b.get("growth_init", 1.0))
             d.radius_batch = int(b.get("radius_batch", 0))
-            d.flags = 0
+            d.flags = _lib.PRC_FLAG_FAITHFUL_WINDOW if b.get("faithful_window") else 0
         self._b = ctypes.c_void_p()
         check(L.prc_d2z_batch_create(self.n, descs, int(n_streams), ctypes.byref(self._b)))
 

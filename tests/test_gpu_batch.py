@@ -75,6 +75,31 @@ def test_grouped_batch_argmax_new_pointers_and_radius_batches():
     batch.close()
 
 
+def test_grouped_batch_with_a_faithful_window_box():
+    """A box asking for the faithful float window is left out of the grouped
+    launches of its size (they use the accurate window) and runs per box
+    inside the same graph: its result equals a faithful single call, and the
+    other boxes of its size still match theirs."""
+    import torch
+    spec = [(32, 6), (32, 7), (64, 5)]
+    boxes, fields_ = zip(*[_box(N, nr, 400 + i) for i, (N, nr) in enumerate(spec)])
+    boxes = [dict(b) for b in boxes]
+    boxes[1]["faithful_window"] = True
+    ref = []
+    for b, d in zip(boxes, fields_):
+        with prc_d2z.Delta2Zreion(b["N"], b["box_mpc"], b["radii_mpc"], b["barrier_b"], b["barrier_a"],
+                                  b["growth_init"], faithful_window=b.get("faithful_window", False)) as ctx:
+            ref.append(ctx.forward(d, want_argmax=False)[0])
+    batch = prc_d2z.Batch(boxes, n_streams=2)
+    dev = [torch.from_numpy(d).cuda() for d in fields_]
+    out = [torch.empty_like(x) for x in dev]
+    batch.forward(dev, out, mode="grouped")
+    torch.cuda.synchronize()
+    for r, o in zip(ref, out):
+        assert np.array_equal(o.cpu().numpy(), r)
+    batch.close()
+
+
 def test_grouped_batch_rejects_partial_argmax():
     import torch
     boxes, fields_ = zip(*[_box(N, nr, 300 + i) for i, (N, nr) in enumerate([(32, 5), (64, 6)])])
