@@ -166,17 +166,6 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   if constexpr (MODE == TM_WIN || MODE == TM_ACC) stage_params(s_kr, a.kr);
   PlanRun<P>::template fill<1>(tws, a.tw);
   __syncthreads();
-  // window pass: 1/(dk R_b)^3 per radius (the spectrum tile is divided by
-  // |m|^3 once, so that a radius needs no reciprocal cube per element)
-  constexpr bool CUBE = (MODE == TM_WIN && V != kWinFaithful);
-  __shared__ float s_c1[CUBE && !MB ? kMaxBatch : 1];
-  if constexpr (CUBE && !MB) {
-    for (int i = threadIdx.x; i < kMaxBatch; i += blockDim.x) {
-      const float kr = s_kr[i];
-      s_c1[i] = __fdiv_rn(1.0f, kr * kr * kr);
-    }
-    __syncthreads();
-  }
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, c = lane & (T - 1);
   int t;
   if constexpr (T == 16) {
@@ -271,36 +260,12 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   };
   // rows m > E/2 mirror rows of the partner lane (lane ^ 16, FFT lane G - t,
   // register E-1-m) or of this lane (t = 0: E-m; t = G/2: E-1-m)
-  // (lanes t = 0 and t = G/2 exist only in warp 0, so the other warps skip
-  // the selects)
   auto mirror = [&](float (&wv)[E]) {
-    if (wp == 0) {
 #pragma unroll
-      for (int m = EH + 1; m < E; ++m) {
-        const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
-        wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
-      }
-    } else {
-#pragma unroll
-      for (int m = EH + 1; m < E; ++m) wv[m] = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
+    for (int m = EH + 1; m < E; ++m) {
+      const float o = __shfl_xor_sync(0xffffffffu, wv[E - 1 - m], 16);
+      wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
     }
-  };
-  // W(|k| R_b) |m|^3 of all E rows for a tile divided by |m|^3 (see
-  // CUBE): 3 (sin x - x cos x) / (dk R_b)^3 for x >= 1 and x^3 times the
-  // Taylor series below 1; c1 = 1/(dk R_b)^3
-  // kmin: the smallest kq of the warp (the Taylor branch runs iff kmin kr < 1)
-  auto wvals_cube = [&](const float (&kq)[EH + 1], float kmin, float kr, float c1, float (&wv)[E]) {
-    const float c3 = 3.0f * c1;
-#pragma unroll
-    for (int m = 0; m <= EH; ++m) wv[m] = tophat_num(kq[m] * kr) * c3;
-    if (kmin * kr < 1.0f) {
-#pragma unroll
-      for (int m = 0; m <= EH; ++m) {
-        const float x = kq[m] * kr;
-        if (x < 1.0f) wv[m] = (x * x * x) * tophat_small(x) * c1;
-      }
-    }
-    mirror(wv);
   };
   // W(|k| R_b) of all E rows
   // (the Taylor branch runs only in warps where some lane needs it)
@@ -366,7 +331,6 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
       float kq[FW ? E : EH + 1];
-      float kmin = 0.f;
       if constexpr (FW) {
         const int col = w.tc * T + c;
         const int iy = sg_nyq(w) ? col : w.outer, iz = sg_nyq(w) ? H : col;
@@ -374,34 +338,17 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         for (int m = 0; m < E; ++m) kq[m] = rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax);
       } else {
         kmag(w, kq);
-        // the tile divided by |m|^3 once (0 at k = 0, where W is 0)
-        float sc[E];
-#pragma unroll
-        for (int m = 0; m <= EH; ++m) sc[m] = kq[m] < 0.f ? 0.f : __fdiv_rn(1.0f, kq[m] * kq[m] * kq[m]);
-        mirror(sc);
-#pragma unroll
-        for (int m = 0; m < E; ++m) raw[m] = cscale(raw[m], sc[m]);
-        kmin = kq[0];
-#pragma unroll
-        for (int m = 1; m <= EH; ++m) kmin = fminf(kmin, kq[m]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) kmin = fminf(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
       }
       auto radius = [&](int b, bool last) {
         float wv[E];
-        float krb, c1;
-        if constexpr (MB) {
-          krb = __ldg(&a.box[w.bx].kr[b]);
-          c1 = __fdiv_rn(1.0f, krb * krb * krb);
-        } else {
-          krb = s_kr[b];
-          if constexpr (CUBE) c1 = s_c1[b];
-        }
+        float krb;
+        if constexpr (MB) krb = __ldg(&a.box[w.bx].kr[b]);
+        else krb = s_kr[b];
         if constexpr (FW) {
 #pragma unroll
           for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
         } else {
-          wvals_cube(kq, kmin, krb, c1, wv);
+          wvals(kq, krb, wv);
         }
         float2 v[E];
 #pragma unroll

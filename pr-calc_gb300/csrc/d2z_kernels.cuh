@@ -207,17 +207,13 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
-// sin x - x cos x for x >= 1 (the reduction and SFU functions as above)
-__device__ __forceinline__ float tophat_num(float x) {
+__device__ __forceinline__ float tophat_big(float x) {
   const float k = rintf(x * 0.159154943091895336f);
   float r = fmaf(-k, 6.28318548202514648f, x);
   r = fmaf(-k, -1.74845560e-07f, r);
   const float s = __sinf(r), c = __cosf(r);
-  return fmaf(-x, c, s);
-}
-__device__ __forceinline__ float tophat_big(float x) {
   const float ix = rcp_approx(x);
-  return 3.0f * tophat_num(x) * (ix * ix * ix);
+  return 3.0f * fmaf(-x, c, s) * (ix * ix * ix);
 }
 __device__ __forceinline__ float tophat(float x) { return x < 1.0f ? tophat_small(x) : tophat_big(x); }
 
