@@ -267,17 +267,23 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       wv[m] = (t == 0) ? wv[E - m] : (t == G / 2 ? wv[E - 1 - m] : o);
     }
   };
-  // W(|k| R_b) of all E rows
-  // (the Taylor branch runs only in warps where some lane needs it)
-  auto wvals = [&](const float (&kq)[EH + 1], float kr, float (&wv)[E]) {
-    bool small = false;
+  // the smallest kq of the warp
+  auto warp_kmin = [&](const float (&kq)[EH + 1]) {
+    float k = kq[0];
 #pragma unroll
-    for (int m = 0; m <= EH; ++m) {
-      const float x = kq[m] * kr;
-      wv[m] = tophat_big(x);
-      small |= (x < 1.0f);
-    }
-    if (__any_sync(0xffffffffu, small)) {
+    for (int m = 1; m <= EH; ++m) k = fminf(k, kq[m]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) k = fminf(k, __shfl_xor_sync(0xffffffffu, k, o));
+    return k;
+  };
+  // W(|k| R_b) of all E rows.  The Taylor branch runs only in warps where
+  // some lane needs it: where kmin kr < 1, kmin the warp's smallest kq (-1
+  // where the warp holds k = 0, which then always takes it, as a per-lane
+  // test would; the result is the same, row by row).
+  auto wvals = [&](const float (&kq)[EH + 1], float kmin, float kr, float (&wv)[E]) {
+#pragma unroll
+    for (int m = 0; m <= EH; ++m) wv[m] = tophat_big(kq[m] * kr);
+    if (kmin * kr < 1.0f) {
 #pragma unroll
       for (int m = 0; m <= EH; ++m) {
         const float x = kq[m] * kr;
@@ -331,6 +337,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
     for (; ti < tiles; ti += gridDim.x) {
       const Where w = where(ti);
       float kq[FW ? E : EH + 1];
+      float kmin = 0.f;
       if constexpr (FW) {
         const int col = w.tc * T + c;
         const int iy = sg_nyq(w) ? col : w.outer, iz = sg_nyq(w) ? H : col;
@@ -338,6 +345,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         for (int m = 0; m < E; ++m) kq[m] = rk_faithful(t + G * m, iy, iz, N, a.dk, a.kmax);
       } else {
         kmag(w, kq);
+        kmin = warp_kmin(kq);
       }
       auto radius = [&](int b, bool last) {
         float wv[E];
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
 #pragma unroll
           for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
         } else {
-          wvals(kq, krb, wv);
+          wvals(kq, kmin, krb, wv);
         }
         float2 v[E];
 #pragma unroll
@@ -376,6 +384,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
       const Where w = where(ti);
       float kq[EH + 1];
       kmag(w, kq);
+      const float kmin = warp_kmin(kq);
       float2 acc[E];
 #pragma unroll
       for (int m = 0; m < E; ++m) acc[m] = make_float2(0.f, 0.f);
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         gload(sg_in(w) + w.off + (long long)b * a.slot_stride, sg_rs(w), v);
         PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
         float wv[E];
-        wvals(kq, s_kr[b], wv);
+        wvals(kq, kmin, s_kr[b], wv);
 #pragma unroll
         for (int m = 0; m < E; ++m) {
           acc[m].x = fmaf(wv[m], v[m].x, acc[m].x);

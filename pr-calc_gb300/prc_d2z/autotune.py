@@ -57,7 +57,7 @@ def _save(path, data):
 
 def candidates(N: int, n_radii: int):
     """(radius batches, window variants) tried for a grid side N."""
-    top = 16 if N >= 1024 else 32         # a 1024^3 slot is 4.3 GB
+    top = 12 if N >= 1024 else 64         # a 1024^3 slot is 4.3 GB
     batches = sorted({min(b, n_radii) for b in (4, 8, 12, 16, 24, 32, 48, 64) if b <= top})
     return batches, list(range(win_variants(N)))
 

@@ -104,14 +104,14 @@ def test_tables_reject_radius_counts_the_reference_does_not_check(nscales):
 
 
 def test_autotuner_candidates_and_cache_path(monkeypatch, tmp_path):
-    """The tuner's search space (radius batches up to the kernels' 32, at most
-    16 at 1024 where a slot is 4.3 GB, never above the radius count; every
+    """The tuner's search space (radius batches up to the kernels' 64, at most
+    12 at 1024 where a slot is 4.3 GB, never above the radius count; every
     compiled window variant) and its cache location, without a GPU."""
     from prc_d2z import autotune
     b, v = autotune.candidates(512, 64)
-    assert b == [4, 8, 12, 16, 24, 32] and v == list(range(prc_d2z.win_variants(512)))
+    assert b == [4, 8, 12, 16, 24, 32, 48, 64] and v == list(range(prc_d2z.win_variants(512)))
     b, _ = autotune.candidates(1024, 96)
-    assert max(b) == 16
+    assert max(b) == 12
     b, _ = autotune.candidates(128, 10)
     assert b == [4, 8, 10]
     assert prc_d2z.win_variants(100) == 0
