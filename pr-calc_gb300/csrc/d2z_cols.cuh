@@ -280,19 +280,24 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
   // some lane needs it: where kmin kr < 1, kmin the warp's smallest kq (-1
   // where the warp holds k = 0, which then always takes it, as a per-lane
   // test would; the result is the same, row by row).
-  auto wvals = [&](const float (&kq)[EH + 1], float kmin, float kr, float (&wv)[E]) {
+  // zero_in_taylor: k = 0 (kq = -1) makes kmin negative, so its warp always
+  // takes the Taylor branch, and W(0) = 0 is set there; otherwise after it,
+  // row by row (the accumulate pass keeps that form: it holds fewer registers)
+  auto wvals = [&](const float (&kq)[EH + 1], float kmin, float kr, float (&wv)[E], bool zero_in_taylor) {
 #pragma unroll
     for (int m = 0; m <= EH; ++m) wv[m] = tophat_big(kq[m] * kr);
     if (kmin * kr < 1.0f) {
 #pragma unroll
       for (int m = 0; m <= EH; ++m) {
         const float x = kq[m] * kr;
-        if (x < 1.0f) wv[m] = tophat_small(x);
+        if (x < 1.0f) wv[m] = (zero_in_taylor && kq[m] < 0.f) ? 0.f : tophat_small(x);
       }
     }
+    if (!zero_in_taylor) {
 #pragma unroll
-    for (int m = 0; m <= EH; ++m)
-      if (kq[m] < 0.f) wv[m] = 0.f;
+      for (int m = 0; m <= EH; ++m)
+        if (kq[m] < 0.f) wv[m] = 0.f;
+    }
     mirror(wv);
   };
 
@@ -356,7 +361,8 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
 #pragma unroll
           for (int m = 0; m < E; ++m) wv[m] = window_faithful(kq[m], krb);
         } else {
-          wvals(kq, kmin, krb, wv);
+          // (at N = 1024 the folded form costs 8 bytes of spills: keep the other)
+          wvals(kq, kmin, krb, wv, N != 1024);
         }
         float2 v[E];
 #pragma unroll
@@ -393,7 +399,7 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         gload(sg_in(w) + w.off + (long long)b * a.slot_stride, sg_rs(w), v);
         PlanRun<P>::template run<false, KK::PP>(v, buf, t, tws, sync);
         float wv[E];
-        wvals(kq, kmin, s_kr[b], wv);
+        wvals(kq, kmin, s_kr[b], wv, false);
 #pragma unroll
         for (int m = 0; m < E; ++m) {
           acc[m].x = fmaf(wv[m], v[m].x, acc[m].x);
