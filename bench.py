@@ -23,7 +23,9 @@ time at 256^3 x 64, loss mean((z - z_t)^2)), "batched" (96 boxes of
 64..256^3 in one captured launch against a per-box loop of the plain path,
 bit-identity checked) and "step_frac" (the whole step's rate on the kernels'
 own algorithmic bytes, on the compulsory floor and on the canonical 3-pass
-model, each against the measured HBM copy rate).
+model, each against the measured HBM copy rate).  "batched" also carries
+"small_boxes": 96 boxes of 64^3, where the per-box loop is bound by launches
+and tails rather than by the kernels.
 
 --impl reference times the CPU implementation of the same step (the oracle's
 faithful-fp32 restatement: scipy.fft with all host threads plus the OpenMP
@@ -389,6 +391,11 @@ def run_ours(args, rank, world, local_rank):
         # the metric's other two parts, each under its own clock record
         out["adjoint"] = adjoint_measure(256, steps=5, warmup=3)
         out["batched"] = batched_measure(steps=5, warmup=3, streams=0)
+        # north star (b): small boxes batched against the per-box loop
+        sb = batched_measure(steps=5, warmup=3, streams=0, small_only=True)
+        out["batched"]["small_boxes"] = {k: sb[k] for k in ("workload", "ms_per_step", "value", "per_box_loop",
+                                                            "per_box_graph", "speedup_vs_loop",
+                                                            "identical_to_loop", "gpu_launches", "clocks")}
     if world == 1 and not args.no_cpu:
         from oracle import d2z_ref as orc  # noqa: F401
         threads = os.cpu_count() or 1
@@ -414,22 +421,23 @@ def _cfg_box(N, nr, seed, zeta, box=None, rmax=RMAX):
                 barrier_b=t.barrier_b, barrier_a=t.barrier_a, growth_init=t.DInit), box
 
 
-def batched_measure(steps, warmup, streams):
+def batched_measure(steps, warmup, streams, small_only=False):
     """96 realisations, grids 64/96/128/192/256 at 1.5 Mpc/h cells, 24-48 radii
-    each: a per-box loop of the plain path, the same launches captured in one
-    graph, and grouped launches (one launch per pass and grid size).  Every box
-    sweeps all its radii at once (radius batch = its radius count: one read of
-    its spectrum and one write of its zreion, the fastest batch at every size)
-    with the autotuned window-pass variant of its grid size; each batch mode
-    picks its stream count by timing.  The modes run one after another, each
-    freeing its workspaces before the next.  Returns a dict (times, speed-ups,
+    each (small_only: 96 boxes of 64^3), seeds 1000..1095: a per-box loop of
+    the plain path, the same launches captured in one graph, and grouped
+    launches (one launch per pass and grid size).  Every box sweeps all its
+    radii at once (radius batch = its radius count: one read of its spectrum
+    and one write of its zreion, the fastest batch at every size) with the
+    autotuned window-pass variant of its grid size; each batch mode picks its
+    stream count by timing.  The modes run one after another, each freeing its
+    workspaces before the next.  Returns a dict (times, speed-ups,
     bit-identity, clocks)."""
     import torch
 
     import prc_d2z
     from prc_d2z import autotune, fields
     rng = np.random.default_rng(2024)
-    sizes = [64] * 20 + [96] * 19 + [128] * 19 + [192] * 19 + [256] * 19
+    sizes = [64] * 96 if small_only else [64] * 20 + [96] * 19 + [128] * 19 + [192] * 19 + [256] * 19
     rng.shuffle(sizes)
     nrs = rng.integers(24, 49, len(sizes))
     boxes, deltas = [], []
@@ -497,8 +505,9 @@ def batched_measure(steps, warmup, streams):
         del outs
         torch.cuda.empty_cache()
     g = res["grouped"]
-    out = {"workload": "96 boxes, N in {64,96,128,192,256} (20/19/19/19/19), 1.5 Mpc/h cells, "
-                       "radii U{24..48} from 2 cells to 60 Mpc/h", "zeta": ZETA_BATCH,
+    mix = "N = 64 (96 boxes)" if small_only else "N in {64,96,128,192,256} (20/19/19/19/19)"
+    out = {"workload": f"96 boxes, {mix}, 1.5 Mpc/h cells, radii U{{24..48}} from 2 cells to 60 Mpc/h",
+           "zeta": ZETA_BATCH,
            "mode": "grouped: one launch per pass over all boxes of a grid size, sizes side by side, one graph",
            "radius_batch": "each box's radius count (one sweep per box)",
            "steps": steps, "warmup": warmup, "ms_per_step": g["ms_per_step"], "value": g["value"], "unit": UNIT,
