@@ -614,6 +614,9 @@ def main():
     _use_config(args.config)
     if args.n == 0:
         args.n = N_DEF
+    elif args.n != N_DEF:
+        global METRIC
+        METRIC = f"zreion cell*radii/s at {args.n}^3 ({NR} radii)"
     if args.workload == "batched" and args.impl == "ours":
         run_batched(args)
         return

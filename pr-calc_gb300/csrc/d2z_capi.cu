@@ -26,7 +26,8 @@
 namespace prc {
 #define PRC_DECL(NV) const KernelSet* kernel_set_##NV();
 PRC_DECL(8) PRC_DECL(12) PRC_DECL(16) PRC_DECL(24) PRC_DECL(32) PRC_DECL(48) PRC_DECL(64)
-PRC_DECL(96) PRC_DECL(128) PRC_DECL(192) PRC_DECL(256) PRC_DECL(512) PRC_DECL(1024)
+PRC_DECL(96) PRC_DECL(128) PRC_DECL(192) PRC_DECL(256) PRC_DECL(384) PRC_DECL(512) PRC_DECL(768)
+PRC_DECL(1024)
 #undef PRC_DECL
 
 // Test hook (prc_d2z_test_withhold_copy): how many forward calls still run
@@ -53,7 +54,9 @@ const KernelSet* kernel_set(int N) {
     case 128: return kernel_set_128();
     case 192: return kernel_set_192();
     case 256: return kernel_set_256();
+    case 384: return kernel_set_384();
     case 512: return kernel_set_512();
+    case 768: return kernel_set_768();
     case 1024: return kernel_set_1024();
     default: return nullptr;
   }

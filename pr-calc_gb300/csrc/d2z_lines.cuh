@@ -40,7 +40,9 @@ template <> struct PCfg<96> : PDef { static constexpr bool on = true; using P = 
 template <> struct PCfg<128> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
 template <> struct PCfg<192> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
 template <> struct PCfg<256> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
+template <> struct PCfg<384> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; };
 template <> struct PCfg<512> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
+template <> struct PCfg<768> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3, 2>; };
 template <> struct PCfg<1024> {
   static constexpr bool on = true;
   using P = Plan<16, 16, 16, 2>;

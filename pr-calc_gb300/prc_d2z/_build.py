@@ -29,7 +29,8 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCLUDE]
 
-CU_LIB = ["d2z_capi.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu", "inst_e.cu", "d2z_noalloc.cu"]
+CU_LIB = ["d2z_capi.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu", "inst_e.cu", "inst_f.cu",
+          "d2z_noalloc.cu"]
 CPP_LIB = ["errors.cpp", "cosmo.cpp", "history.cpp"]
 CPP_EXE = ["main_d2z.cpp"]
 

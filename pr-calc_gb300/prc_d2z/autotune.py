@@ -57,8 +57,10 @@ def _save(path, data):
 
 def candidates(N: int, n_radii: int):
     """(radius batches, window variants) tried for a grid side N."""
-    top = 12 if N >= 1024 else 64         # a 1024^3 slot is 4.3 GB
-    batches = sorted({min(b, n_radii) for b in (4, 8, 12, 16, 24, 32, 48, 64) if b <= top})
+    # radius slots up to 60 GB (a slot is N^2 (N/2 + 2) complex64: 0.54 GB at
+    # 512, 1.8 GB at 768, 4.3 GB at 1024), so at most 64, 32 and 12 radii
+    slot = N * N * (N // 2 + 2) * 8
+    batches = sorted({min(b, n_radii) for b in (4, 8, 12, 16, 24, 32, 48, 64) if b * slot <= 60e9})
     return batches, list(range(win_variants(N)))
 
 

@@ -30,9 +30,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_supported_sizes():
     s = prc_d2z.supported_sizes()
-    for n in (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512, 1024):
-        assert n in s
-    assert 100 not in s
+    assert s == [8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024]
 
 
 def _desc(N=32, nr=4, **kw):
@@ -104,14 +102,17 @@ def test_tables_reject_radius_counts_the_reference_does_not_check(nscales):
 
 
 def test_autotuner_candidates_and_cache_path(monkeypatch, tmp_path):
-    """The tuner's search space (radius batches up to the kernels' 64, at most
-    12 at 1024 where a slot is 4.3 GB, never above the radius count; every
-    compiled window variant) and its cache location, without a GPU."""
+    """The tuner's search space (radius batches up to the kernels' 64 and to
+    60 GB of slots: at most 32 at 768 and 12 at 1024, where a slot is 1.8 and
+    4.3 GB; never above the radius count; every compiled window variant) and
+    its cache location, without a GPU."""
     from prc_d2z import autotune
     b, v = autotune.candidates(512, 64)
     assert b == [4, 8, 12, 16, 24, 32, 48, 64] and v == list(range(prc_d2z.win_variants(512)))
     b, _ = autotune.candidates(1024, 96)
     assert max(b) == 12
+    b, _ = autotune.candidates(768, 64)
+    assert max(b) == 32
     b, _ = autotune.candidates(128, 10)
     assert b == [4, 8, 10]
     assert prc_d2z.win_variants(100) == 0
