@@ -46,14 +46,14 @@ template <int E, int R0, int... R> struct FirstRadix<Plan<E, R0, R...>> { static
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 template <> struct CCfg<32> { static constexpr bool on = true; using P = Plan<16, 16, 2>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<64> { static constexpr bool on = true; using P = Plan<16, 16, 4>; static constexpr int T = 16, TWIN = 16; };
-template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<96> { static constexpr bool on = true; using P = Plan<12, 12, 4, 2>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<128> { static constexpr bool on = true; using P = Plan<16, 16, 8>; static constexpr int T = 16, TWIN = 16; };
-template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<192> { static constexpr bool on = true; using P = Plan<12, 12, 4, 4>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<256> { static constexpr bool on = true; using P = Plan<16, 16, 16>; static constexpr int T = 16, TWIN = 16; };
-template <> struct CCfg<384> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3, 2>; static constexpr int T = 16, TWIN = 16; };
+template <> struct CCfg<384> { static constexpr bool on = true; using P = Plan<12, 12, 4, 4, 2>; static constexpr int T = 16, TWIN = 16; };
 template <> struct CCfg<512> { static constexpr bool on = true; using P = Plan<16, 16, 16, 2>; static constexpr int T = 16, TWIN = 8; };
 // N = 768: 64 lanes x 8 columns, as at 1024.
-template <> struct CCfg<768> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 4, 3>; static constexpr int T = 8, TWIN = 8; };
+template <> struct CCfg<768> { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 12>; static constexpr int T = 8, TWIN = 8; };
 // N = 1024: 64 lanes x 8 columns in every pass.  (Measured no faster: plain
 // passes on 32 lanes x 16 columns with 32 elements a lane, and on 64 lanes x 16
 // columns in 1024-thread CTAs of 64 registers -- both 128-byte rows, one

@@ -38,13 +38,13 @@ template <> struct LCfg<24> { using P = Plan<12, 4, 3>; };
 template <> struct LCfg<32> { using P = Plan<8, 8, 2>; };
 template <> struct LCfg<48> { using P = Plan<12, 4, 3, 2>; };
 template <> struct LCfg<64> { using P = Plan<8, 8, 4>; };
-template <> struct LCfg<96> { using P = Plan<12, 4, 4, 3>; };
+template <> struct LCfg<96> { using P = Plan<12, 12, 4>; };
 template <> struct LCfg<128> { using P = Plan<8, 8, 8>; };
-template <> struct LCfg<192> { using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct LCfg<192> { using P = Plan<12, 12, 4, 2>; };
 template <> struct LCfg<256> { using P = Plan<8, 8, 4, 4>; };
-template <> struct LCfg<384> { using P = Plan<12, 4, 4, 4, 3>; };
+template <> struct LCfg<384> { using P = Plan<12, 12, 4, 4>; };
 template <> struct LCfg<512> { using P = Plan<8, 8, 8, 4>; };
-template <> struct LCfg<768> { using P = Plan<12, 4, 4, 4, 3, 2>; };
+template <> struct LCfg<768> { using P = Plan<12, 12, 4, 4, 2>; };
 template <> struct LCfg<1024> { using P = Plan<8, 8, 8, 8>; };
 
 // Tile plan (length N), tile width T (columns; T divides N/2 and N) and the

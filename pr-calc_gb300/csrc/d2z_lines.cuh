@@ -36,13 +36,13 @@ template <int N> struct PCfg { static constexpr bool on = false; };
 struct PDef { static constexpr int THREADS = 128, MINB = 4; };
 template <> struct PCfg<32> : PDef { static constexpr bool on = true; using P = Plan<8, 8, 2>; };
 template <> struct PCfg<64> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 2>; };
-template <> struct PCfg<96> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 3>; };
+template <> struct PCfg<96> : PDef { static constexpr bool on = true; using P = Plan<12, 12, 4>; };
 template <> struct PCfg<128> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 4>; };
-template <> struct PCfg<192> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 2, 3>; };
+template <> struct PCfg<192> : PDef { static constexpr bool on = true; using P = Plan<12, 12, 4, 2>; };
 template <> struct PCfg<256> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 8>; };
-template <> struct PCfg<384> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3>; };
+template <> struct PCfg<384> : PDef { static constexpr bool on = true; using P = Plan<12, 12, 4, 4>; };
 template <> struct PCfg<512> : PDef { static constexpr bool on = true; using P = Plan<16, 16, 16>; };
-template <> struct PCfg<768> : PDef { static constexpr bool on = true; using P = Plan<12, 4, 4, 4, 3, 2>; };
+template <> struct PCfg<768> : PDef { static constexpr bool on = true; using P = Plan<12, 12, 4, 4, 2>; };
 template <> struct PCfg<1024> {
   static constexpr bool on = true;
   using P = Plan<16, 16, 16, 2>;
