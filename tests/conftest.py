@@ -32,3 +32,17 @@ def pytest_collection_modifyitems(config, items):
     for it in items:
         if "gpu" in it.keywords:
             it.add_marker(skip)
+
+
+@pytest.fixture(autouse=True)
+def _release_device_memory(request):
+    """After each GPU test, hand torch's cached device blocks back to the
+    driver, so that the next test's free-memory check (the full-size tests
+    need 24-110 GB) sees what is really free."""
+    yield
+    if "gpu" in request.keywords and _have_gpu():
+        import gc
+
+        import torch
+        gc.collect()
+        torch.cuda.empty_cache()
