@@ -2,7 +2,7 @@
 // and H a multiple of the tile width).
 //
 // A tile is T adjacent columns x N rows (T = 16; 8 in the window pass at
-// N = 512 and in every pass at N = 1024).  Thread
+// N = 512 and in every pass at N = 768 and 1024).  Thread
 // (t, c) of a CTA of T*G threads holds rows t + G*m (m < E) of column c in
 // registers: T lanes of a warp are the T columns of one row, so every global
 // load and store is a whole row segment (128 or 64 bytes) and the data go
