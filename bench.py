@@ -29,7 +29,11 @@ and tails rather than by the kernels.
 
 --impl reference times the CPU implementation of the same step (the oracle's
 faithful-fp32 restatement: scipy.fft with all host threads plus the OpenMP
-C loops of oracle/d2z_cells.c): every step is a whole step, all radii.
+C loops of oracle/d2z_cells.c): every step is a whole step, all radii, while
+the K steps fit in REF_BUDGET_S seconds of CPU time; beyond that each step is
+the forward R2C plus an evenly spread sample of the radii, scaled to all of
+them (the cost per radius does not depend on the radius), and the line says
+which.
 """
 from __future__ import annotations
 
@@ -56,6 +60,7 @@ MMIN_MSUN = 1e9 / H_
 # zeta from prc_d2z.calibrate: raw zreion with x_i(z=8) = 0.5 at seed 1
 ZETA = 80.5404       # 512^3, 600 Mpc/h, 64 radii to 60 Mpc/h
 ZETA_BATCH = 81.6855 # 256^3, 384 Mpc/h (1.5 Mpc/h cells), 48 radii to 60 Mpc/h
+REF_BUDGET_S = 600.0 # reference arm: CPU seconds for the K timed steps (whole steps at K = 20)
 # plain configurations: N, box [Mpc/h], radii, calibrated zeta (x_i(z=8) = 0.5 at seed 1)
 CONFIGS = {"C1": (128, 200.0, 32, 82.4429), "C2": (512, 600.0, 64, 80.5404), "C3": (1024, 1200.0, 96, 73.1587)}
 
@@ -220,13 +225,21 @@ def run_reference(args, rank):
     delta = fields.gaussian_field(N, p.BoxSize, seed=1)
     box_mpc = float(np.float32(p.BoxSize) / np.float32(H_))
     vals = []
-    for s in range(args.warmup):  # warm-up: the FFT plans, thread pools and caches (not timed)
-        cpu_sample(delta, T, box_mpc, 2, threads)
+    warm = None
+    for s in range(max(1, args.warmup)):  # warm-up: the FFT plans, thread pools and caches (not timed)
+        warm = cpu_sample(delta, T, box_mpc, 2, threads)
+    # radii per step: all of them (whole steps) while K whole steps fit in
+    # REF_BUDGET_S, else as many as fit, evenly spread over the radius grid
+    nr_s = args.ref_radii
+    if nr_s <= 0:
+        t_fwd, t_rad = warm[1], warm[2]
+        fit = int((REF_BUDGET_S / max(1, args.steps) - t_fwd) / max(t_rad, 1e-9))
+        nr_s = max(2, min(NR, fit))
+    nr_s = min(nr_s, NR)
     for s in range(args.steps):
-        vals.append(cpu_sample(delta, T, box_mpc, args.ref_radii or NR, threads))
+        vals.append(cpu_sample(delta, T, box_mpc, nr_s, threads))
     v = statistics.median(x[0] for x in vals)
     ms = N ** 3 * NR / v * 1e3
-    nr_s = args.ref_radii or NR
     if nr_s >= NR:
         sample = (f"whole steps: forward R2C + all {NR} radii at {N}^3 "
                   f"(t_fwd {statistics.median(x[1] for x in vals):.2f} s, "
@@ -612,7 +625,9 @@ def main():
     ap.add_argument("--config", default="C2", choices=sorted(CONFIGS))
     ap.add_argument("--n", type=int, default=0, help="grid side (default: the config's; keeps its cell size)")
     ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--ref-radii", type=int, default=0, help="reference arm: radii per step (0: all, a whole step)")
+    ap.add_argument("--ref-radii", type=int, default=0,
+                    help="reference arm: radii per step (0: all of them, a whole step, while the K steps fit in "
+                         f"{REF_BUDGET_S:g} s; else as many as fit)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="default line without the adjoint and batched parts")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"])
