@@ -398,6 +398,13 @@ void run_tile(prc_d2z_ctx* c, int mode, TileSeg s0, TileSeg s1, int gy, int nb =
                 : faithful         ? c->ksl.occ_win_faithful
                 : (mode == TM_WIN) ? c->ksl.occ_winv[wv] : c->ksl.occ_tile;
   dim3 grid(grid_for(tiles, 1, occ, c->sms), gy, 1);
+  if (mode == TM_WIN && c->N <= 128) {
+    // fewer tiles than two waves of resident CTAs: the sweep's radii are
+    // split over blockIdx.y as well (the kernels of grids up to 128 read
+    // their radius range from it)
+    const long long want = 2LL * occ * c->sms;
+    if (tiles < want) grid.y = (unsigned)std::min<long long>(nb, (want + tiles - 1) / tiles);
+  }
   const int kind = mode == TM_FWD ? PRC_KIND_COL_FWD
                  : mode == TM_INV ? PRC_KIND_COL_INV
                  : mode == TM_WIN ? PRC_KIND_WIN_X : PRC_KIND_ADJ_X;

@@ -137,6 +137,12 @@ template <> struct WinVar<512, 2> : WinDef { static constexpr bool on = true; st
 constexpr int kWinFaithful = 7;
 template <int N> struct WinVar<N, kWinFaithful> : WinVar<N, 0> {};
 
+// Grid sizes whose window pass may split a sweep's radii over blockIdx.y
+// (radius_range): up to 128, where the tiles do not fill two waves of CTAs.
+// Larger grids keep the plain loop (at 512 the split's extra live register
+// would make the window pass spill).
+template <int N> constexpr bool kWinRadiusSplit = N <= 128;
+
 // Tile width and plan of a mode: the window pass uses its variant V, and the
 // accumulate mode uses variant 0 of the window pass when the plain plan holds
 // more than 16 elements a lane (its accumulator would not fit beside them).
@@ -382,11 +388,12 @@ __global__ void __launch_bounds__(ColK<N, MODE, V>::type::THREADS, ColK<N, MODE,
         gstore(w, sg_out(w) + (long long)b * a.slot_stride, v);
       };
       // the last radius is peeled so that kq's and raw's live ranges end before it
-      int nbt;
-      if constexpr (MB) nbt = __ldg(&a.box[w.bx].nb);
-      else nbt = a.nb;
-      for (int b = 0; b < nbt - 1; ++b) radius(b, false);
-      radius(nbt - 1, true);
+      int b0 = 0, b1;
+      if constexpr (MB) b1 = __ldg(&a.box[w.bx].nb);
+      else if constexpr (kWinRadiusSplit<N>) radius_range(a.nb, b0, b1);
+      else b1 = a.nb;
+      for (int b = b0; b < b1 - 1; ++b) radius(b, false);
+      radius(b1 - 1, true);
     }
   } else {  // TM_ACC (output never transposed)
     for (int ti = blockIdx.x; ti < tiles; ti += gridDim.x) {

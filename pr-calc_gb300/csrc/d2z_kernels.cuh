@@ -267,6 +267,15 @@ __device__ __forceinline__ void stage_params(float* dst, const float (&src)[kMax
   }
 }
 
+// Radii [b0, b1) of this CTA in a window pass: the sweep's nb radii split
+// evenly over gridDim.y (gridDim.y <= nb, so no range is empty).  Small grids
+// have fewer tiles than the GPU holds CTAs; splitting the radii gives every SM
+// work (each radius of a tile is computed the same way in any split).
+__device__ __forceinline__ void radius_range(int nb, int& b0, int& b1) {
+  b0 = (int)((long long)blockIdx.y * nb / gridDim.y);
+  b1 = (int)((long long)(blockIdx.y + 1) * nb / gridDim.y);
+}
+
 // ------------------------------------------------------------ tiles
 // A T-column tile is cut into 128-byte lines of 16 float2 words (16/T rows
 // each); word w of line l is stored at l*16 + (w ^ f(l)),
@@ -573,13 +582,15 @@ __global__ void __launch_bounds__(TK<N>::THREADS, MODE == TM_ACC ? TK<N>::MINB_A
       io.load_async(raw, w0.sg.in + w0.off, w0.sg.row_stride);
     }
     cp_async_commit();
+    int b0, b1;
+    radius_range(a.nb, b0, b1);
     for (; ti < tiles; ti += gridDim.x) {
       cp_async_wait<0>();
       __syncthreads();
-      for (int b = 0; b < a.nb; ++b) {
+      for (int b = b0; b < b1; ++b) {
         float2 v[E];
         col_read(raw, v);
-        if (b == a.nb - 1) {
+        if (b == b1 - 1) {
           // every group has its raw column: stream the next spectrum tile in
           __syncthreads();
           const int tn = ti + gridDim.x;
