@@ -221,7 +221,11 @@ struct prc_d2z_ctx {
   float* gstage = nullptr;
   uint8_t* amstage = nullptr;
   float* grf_amp = nullptr;       // field generator: amplitude by |m|^2
-  int* err = nullptr;             // set by a kernel whose copy wait ran out
+  // set by a kernel whose copy wait ran out: one word of pinned host memory
+  // mapped into the device (err its device address, err_h the host's), so
+  // that the host reads it after the stream synchronisation without a copy
+  int* err = nullptr;
+  int* err_h = nullptr;
   // prc_d2z_forward_many: two device copies of a box's input and outputs and
   // two copy streams (in, out), so that the copies of neighbouring boxes run
   // on the copy engines while this box's kernels run
@@ -321,7 +325,7 @@ void free_all(prc_d2z_ctx* c) {
   cudaFree(c->gstage);
   cudaFree(c->amstage);
   cudaFree(c->grf_amp);
-  cudaFree(c->err);
+  if (c->err_h) cudaFreeHost(c->err_h);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (int k = 0; k < 2; ++k) {
@@ -838,17 +842,18 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
       (st = dalloc(&c->tw, (size_t)c->N, "twiddles")) != PRC_OK ||
       (st = dalloc(&c->sig, (size_t)c->nr, "sigma accumulators")) != PRC_OK ||
       (st = dalloc(&c->dB, (size_t)c->nr, "barrier gradient")) != PRC_OK ||
-      (st = dalloc(&c->counts, (size_t)kNHistory, "history counts")) != PRC_OK ||
-      (st = dalloc(&c->err, (size_t)1, "error flag")) != PRC_OK) {
+      (st = dalloc(&c->counts, (size_t)kNHistory, "history counts")) != PRC_OK) {
     free_all(c);
     delete c;
     return st;
   }
-  if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) {
+  if ((e = cudaHostAlloc((void**)&c->err_h, sizeof(int), cudaHostAllocMapped)) != cudaSuccess ||
+      (e = cudaHostGetDevicePointer((void**)&c->err, c->err_h, 0)) != cudaSuccess) {
     free_all(c);
     delete c;
     return cuda_fail(e, "prc_d2z_create: error flag");
   }
+  *c->err_h = 0;
   (void)n3l;
   // twiddles e^{+2 pi i k/N}, FP64 on the host
   std::vector<float2> tw(c->N);
@@ -869,11 +874,12 @@ int prc_d2z_create(const prc_d2z_desc* d, prc_d2z_ctx** out) {
 
 namespace {
 // Reads and clears the context's kernel error flag (after a synchronisation).
+// After the stream synchronisation: the kernels' writes to the mapped word are
+// complete and visible to the host.
 int check_kernel_flag(prc_d2z_ctx* c, const char* who) {
-  int h = 0;
-  PRC_CU(cudaMemcpy(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
-  if (h) {
-    cudaMemset(c->err, 0, sizeof(int));
+  volatile int* h = c->err_h;
+  if (*h) {
+    *h = 0;
     return prc_fail(PRC_ERR_CUDA, "%s: a staging copy did not complete within the wait limit", who);
   }
   return PRC_OK;

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(PK<N>::THREADS, PK<N>::MINB) k_c2r_zp(SweepArg
     // step i staged for everyone; everyone is done reading buffer (i+1) & 1
     if (__syncthreads_or(late)) {
       if (threadIdx.x == 0) {
-        if (a.err) atomicExch(a.err, 1);
+        if (a.err) *reinterpret_cast<volatile int*>(a.err) = 1;  // may be mapped host memory
         // the copy this step waited for may still be landing: wait for it
         // (bounded) before the CTA's shared memory is released
         if (!(withheld && i == 0)) mbar_wait(&s_bar[bi], phase, kWaitPolls);
