@@ -531,7 +531,8 @@ struct prc_d2z_batch {
   // grouped launches
   std::vector<BatchGroup> groups;
   std::vector<cudaEvent_t> gev;  // one join event per group
-  std::vector<char> h_tab;       // host image of the tables
+  char* h_tab = nullptr;         // host image of the tables (pinned: the copy is asynchronous)
+  size_t tab_bytes = 0;
   char* d_tab = nullptr;
   int launches = 0;              // launches of the last grouped forward
 };
@@ -543,6 +544,7 @@ void batch_free(prc_d2z_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (auto e : b->gev) cudaEventDestroy(e);
   cudaFree(b->d_tab);
+  if (b->h_tab) cudaFreeHost(b->h_tab);
   for (auto* c : b->ctx) prc_d2z_destroy(c);
   for (auto e : b->ev) cudaEventDestroy(e);
   for (auto s : b->streams) cudaStreamDestroy(s);
@@ -578,6 +580,9 @@ int batch_group_setup(prc_d2z_batch* b) {
   b->gev.clear();
   cudaFree(b->d_tab);
   b->d_tab = nullptr;
+  if (b->h_tab) cudaFreeHost(b->h_tab);
+  b->h_tab = nullptr;
+  b->tab_bytes = 0;
   std::vector<int> sizes;
   for (auto* c : b->ctx)
     if (groupable(c) && std::find(sizes.begin(), sizes.end(), c->N) == sizes.end()) sizes.push_back(c->N);
@@ -623,10 +628,12 @@ int batch_group_setup(prc_d2z_batch* b) {
     }
     b->groups.push_back(g);
   }
-  b->h_tab.assign(off, 0);
   if (off) {
     int st;
     if ((st = dalloc(&b->d_tab, off, "batch tables")) != PRC_OK) return st;
+    PRC_CU(cudaMallocHost((void**)&b->h_tab, off), "batch tables (host)");
+    memset(b->h_tab, 0, off);
+    b->tab_bytes = off;
   }
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
     b->groups[gi].st = b->streams[gi % b->streams.size()];
@@ -639,7 +646,7 @@ int batch_group_setup(prc_d2z_batch* b) {
 
 // Host image of every group's tables for these inputs and outputs.
 void batch_group_fill(prc_d2z_batch* b, const float* const* delta, float* const* zreion, uint8_t* const* argmax) {
-  char* h = b->h_tab.data();
+  char* h = b->h_tab;
   for (const auto& g : b->groups) {
     for (size_t k = 0; k < g.boxes.size(); ++k) {
       const int i = g.boxes[k];
@@ -1502,9 +1509,12 @@ int prc_d2z_batch_forward(prc_d2z_batch* b, const float* const* delta, float* co
     // kernels are captured with their pointers (recaptured when they change).
     const int gkey = argmax ? 3 : 2;
     if (b->groups.empty() && (st = batch_group_setup(b)) != PRC_OK) return st;
+    // the previous call's table copy has finished reading the host image
+    // (a call synchronises before it returns; this covers one that failed)
+    PRC_CU(cudaStreamSynchronize(b->origin), "prc_d2z_batch_forward");
     batch_group_fill(b, delta, zreion, argmax);
-    if (!b->h_tab.empty())
-      PRC_CU(cudaMemcpyAsync(b->d_tab, b->h_tab.data(), b->h_tab.size(), cudaMemcpyHostToDevice, b->origin),
+    if (b->tab_bytes)
+      PRC_CU(cudaMemcpyAsync(b->d_tab, b->h_tab, b->tab_bytes, cudaMemcpyHostToDevice, b->origin),
              "batch tables");
     std::vector<const void*> key;
     for (int i = 0; i < b->n; ++i)
