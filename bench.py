@@ -120,7 +120,7 @@ class Clocks:
             self.lines = [l for l in out.splitlines() if l.strip()]
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, reasons, watts = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for l in getattr(self, "lines", []):
             f = [x.strip() for x in l.split(",")]
@@ -131,11 +131,16 @@ class Clocks:
                 mx = float(f[2])
             except ValueError:
                 continue
+            try:
+                watts.append(float(f[3]))
+            except ValueError:
+                pass
             for n, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w": round(statistics.median(watts), 1) if watts else None}
 
 
 def _config(N, box):
@@ -339,17 +344,19 @@ def run_ours(args, rank, world, local_rank):
         copy_gbs[kind] = 4 * N ** 3 / (c0.elapsed_time(c1) * 1e6)
     del scratch
     ctx.forward_many([hd, hd], hz)
-    # three streams of K boxes, the median reported: the host link's rate
-    # varies from one moment to the next on a shared machine (the copy
-    # engines measured 117-211 GB/s within one minute)
+    # three streams of K boxes, the median reported: the pipelined rate
+    # varies from run to run on a shared machine (28.3 to 34.0 ms a box for
+    # the same build, the device-resident step taking 28.2-28.4 ms); clocks
+    # and power are sampled over the three
     e2e_reps = []
-    for _ in range(3):
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.forward_many([hd] * args.steps, [hz[i % 2] for i in range(args.steps)])
-        torch.cuda.synchronize()
-        e2e_reps.append(max_over_ranks(time.perf_counter() - t0, device=dev))
+    with Clocks(local_rank) as clk_e2e:
+        for _ in range(3):
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.forward_many([hd] * args.steps, [hz[i % 2] for i in range(args.steps)])
+            torch.cuda.synchronize()
+            e2e_reps.append(max_over_ranks(time.perf_counter() - t0, device=dev))
     e2e_s = statistics.median(e2e_reps)
     e2e = world * N ** 3 * NR * args.steps / e2e_s
 
@@ -397,7 +404,7 @@ def run_ours(args, rank, world, local_rank):
         "tuning": {"radius_batch": B, "win_variant": tuned[1] if tuned else 0, "autotuned": tuned is not None},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * N ** 3, "d2h_bytes_per_step": 4 * N ** 3,
                 "api": "prc_d2z_forward_many (K boxes, pinned host buffers, copies overlapped; median of 3 runs)",
-                "runs_ms_per_box": [round(t / args.steps * 1e3, 3) for t in e2e_reps],
+                "runs_ms_per_box": [round(t / args.steps * 1e3, 3) for t in e2e_reps], "clocks": clk_e2e.summary(),
                 "single_call_value": e2e_single, "copy_engine_gbs": copy_gbs},
         "gpu_launches": launches,
         "roofline": rl,
