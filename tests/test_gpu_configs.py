@@ -2,8 +2,10 @@
 the other tests leave at their defaults: the 128^3 plain configuration exactly
 (200 Mpc/h, 32 radii from 2 cells to 60 Mpc/h, zeta 82.44, M_min 1e9 Msun/h,
 seed 1), a start redshift zInit = 6 (D_init != 1 through the forward R2C and
-the adjoint, main_d2z.C:57-59), and the faithful float window
-(PRC_FLAG_FAITHFUL_WINDOW, delta2zreion_d2z.C:41-43,59-82)."""
+the adjoint, main_d2z.C:57-59), the faithful float window
+(PRC_FLAG_FAITHFUL_WINDOW, delta2zreion_d2z.C:41-43,59-82), and the
+parameters of the reference's own example run (512^3, radii from half a
+cell)."""
 import math
 
 import numpy as np
@@ -175,3 +177,53 @@ def test_faithful_window_on_plane_waves(N):
         if x < 0.02:
             # the faithful window's cancellation is what the flag reproduces
             assert abs(float(wf) - we) > 100 * tol, (x, float(wf), we)
+
+
+def test_reference_example_configuration_against_fp64():
+    """The parameters of the reference's own example run
+    (example/parameterfiles/globalParams.ini, example/runexample.sh): N = 512
+    in a 500 Mpc/h box, 32 radii from half a cell (Rmin 0.5) to the mean free
+    path 140 Mpc/h (-r), zeta 30 (-z), M_min 2e9 Msun (-m), the example's
+    cosmology (h 0.679, Omega_m 0.27, Omega_b 0.044, sigma_8 0.8, n_s 0.972).
+    Half-cell radii put most of the small radii's spectrum in the window's
+    Taylor branch.  delta_R of the first, a middle and the last radius within
+    1e-5 relative RMS of the FP64 chain; zreion within eps_z and the same
+    argmax on every clear cell; x_i(z) within 1e-4."""
+    import torch
+    from fp64_chain import chain
+    free, _ = torch.cuda.mem_get_info()
+    if free < 16 * 2 ** 30:
+        pytest.skip("not enough device memory for the FP64 restatement")
+    cos = dict(Omegam=0.27, Omegab=0.044, Omegal=0.73, h=0.679, ns=0.972, sigma8=0.8)
+    N, box, nr = 512, 500.0, 32
+    p = prc_d2z.Parameters(N=N, Nscales=nr, BoxSize=box, Rmin=0.5, **cos)
+    cl = prc_d2z.CLParameters(Rmax=140.0, zeta=30.0, M_min=2e9)
+    delta = fields.gaussian_field(N, box, seed=18937, backend="torch").contiguous()
+    check = (0, nr // 2, nr - 1)
+    with prc_d2z.Delta2Zreion.from_parameters(p, cl) as ctx:
+        t = ctx.tables
+        box_mpc = float(np.float32(box) / np.float32(cos["h"]))
+        z, am, _ = ctx.forward(delta)
+        dRs = {r: ctx.smooth(delta, r) for r in check}
+        torch.cuda.synchronize()
+        zo, amo, gap, dmax, keep = chain(delta, box_mpc, t.radii_mpc, t.barrier_a, t.barrier_b, t.DInit, check)
+        for r in check:
+            d = dRs[r].double() - keep[r]
+            rel = math.sqrt(float((d * d).mean()) / float((keep[r] * keep[r]).mean()))
+            assert rel < 1e-5, (r, rel)
+        del keep, dRs
+        eps = t.barrier_a * 1e-5 * dmax + 2 * torch.abs(zo).float().nextafter(
+            torch.tensor(math.inf, device=zo.device)).sub(torch.abs(zo).float()).double()
+        clear = gap > eps
+        frac_near = 1.0 - float(clear.double().mean())
+        assert frac_near < 0.05, frac_near
+        dz = (z.double() - zo).abs()
+        assert bool((dz[clear] <= eps[clear]).all()), float(dz[clear].max())
+        assert bool((am[clear] == amo[clear]).all())
+        _, x_64, _ = ctx.history(zo.float().contiguous())
+        _, x_gpu, _ = ctx.history(z)
+        dx = float(np.max(np.abs(x_gpu.astype(np.float64) - x_64.astype(np.float64))))
+        assert dx <= 1e-4, dx
+        print(f"example run: radii {t.radii_mpc[0]:.3f}..{t.radii_mpc[-1]:.1f} Mpc, near-barrier {frac_near:.2e}, "
+              f"max |dz| on clear cells {float(dz[clear].max()):.3e}, max |dx_i| {dx:.2e}, "
+              f"ionised at z=0: {float((z > 0).double().mean()):.3f}")
