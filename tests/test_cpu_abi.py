@@ -51,6 +51,8 @@ def _desc(N=32, nr=4, **kw):
 
 @pytest.mark.parametrize("kw,code", [
     ({"N": 100}, _lib.PRC_ERR_UNSUPPORTED),
+    ({"N": 640}, _lib.PRC_ERR_UNSUPPORTED),
+    ({"N": 2048}, _lib.PRC_ERR_UNSUPPORTED),
     ({"n_radii": 0}, _lib.PRC_ERR_INVALID),
     ({"n_radii": 300}, _lib.PRC_ERR_INVALID),
     ({"box_mpc": 0.0}, _lib.PRC_ERR_INVALID),
