@@ -57,3 +57,27 @@ def test_other_ranks_print_nothing(bench, capsys):
     args = argparse.Namespace(n=16, steps=1, warmup=1, ref_radii=0, gpus=2)
     bench.run_reference(args, 1)
     assert capsys.readouterr().out == ""
+
+
+def test_step_bytes_at_512(monkeypatch):
+    """The roofline arithmetic of the 512^3 x 64 line: the compulsory floor
+    8 N_c + 8 N^3 per radius (103.2 GB), the canonical 3-pass model
+    40 N_c + 8 N^3 per radius plus the forward R2C's 4 N^3 + 40 N_c (241.2 GB
+    + 3.2 GB), and the kernels' own bytes: one sweep of 64 radii reads the
+    spectrum and writes zreion once (142.3 GB), two sweeps of 32 read them
+    twice (143.9 GB)."""
+    monkeypatch.syspath_prepend(REPO)
+    import bench as b
+    b._use_config("C2")
+    N = 512
+    Nc = N * N * (N // 2 + 1)
+    own64, floor, canon = b._step_bytes(N, 64)
+    own32, _, _ = b._step_bytes(N, 32)
+    assert floor == 64 * (8 * Nc + 8 * N ** 3) and abs(floor / 1e9 - 103.21) < 0.01
+    assert canon == 64 * (40 * Nc + 8 * N ** 3) + 4 * N ** 3 + 40 * Nc
+    assert abs((canon - 4 * N ** 3 - 40 * Nc) / 1e9 - 241.19) < 0.01
+    # forward (r2c: 4 N^3 + 8 N_c; two column passes: 16 N_c each), window
+    # (8 N_c + 8 N_c b), y pass (16 N_c b), z pass (8 N_c b + 4 N^3, +4 N^3 a later sweep)
+    fwd = 4 * N ** 3 + 8 * Nc + 32 * Nc
+    assert own64 == fwd + 8 * Nc + 8 * Nc * 64 + 16 * Nc * 64 + 8 * Nc * 64 + 4 * N ** 3
+    assert own32 - own64 == 8 * Nc + 8 * N ** 3
